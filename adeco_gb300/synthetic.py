@@ -1,0 +1,101 @@
+"""Seeded synthetic inputs: Zel'dovich-displaced Lagrangian lattices.
+
+ADECO reads N-body snapshots (Dark Sky files, src/AdPointDataReaders.h); no
+dataset is available here, so the workloads are generated from the recipe
+the benchmark configurations name:
+
+* lattice q = (i+1/2, j+1/2, k+1/2) * L/n, ids x fastest
+  (the SORTED_BY_ID layout, src/AdPointDataReaders.h:770-910);
+* a Gaussian random field delta(k) with P(k) ∝ k^-2 exp(-(k/k_c)^2),
+  k_c = 8 * 2pi / L, from ``numpy.random.default_rng(seed)``;
+* the Zel'dovich displacement psi(k) = i k / k^2 delta(k), rescaled to a
+  stated RMS |psi| in lattice spacings; x = q + psi.
+
+Positions are returned already unwrapped (q + psi, not wrapped into [0, L)):
+that is what the reference's periodic unwrap (``apply_boundary_corrections``,
+src/AdPointDataReaders.h:154-204) reconstructs for displacements below L/4.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def zeldovich_lattice(n: int, L: float = 100.0, seed: int = 0, rms_disp: float = 0.5,
+                      kc_factor: float = 8.0, infall: int = 0, infall_seed: int | None = None,
+                      dtype=np.float32) -> np.ndarray:
+    """Return positions of shape (n, n, n, 3) indexed [k, j, i] (x fastest)."""
+    rng = np.random.default_rng(seed)
+    white = rng.standard_normal((n, n, n))
+    dk = np.fft.rfftn(white)
+    del white
+    kf = 2.0 * np.pi / L
+    kx = np.fft.rfftfreq(n, d=1.0 / n) * kf          # last axis (x) is the rfft axis
+    ky = np.fft.fftfreq(n, d=1.0 / n) * kf
+    kz = np.fft.fftfreq(n, d=1.0 / n) * kf
+    k2 = kz[:, None, None] ** 2 + ky[None, :, None] ** 2 + kx[None, None, :] ** 2
+    kc = kc_factor * kf
+    with np.errstate(divide="ignore", invalid="ignore"):
+        amp = np.where(k2 > 0, np.sqrt(1.0 / k2 * np.exp(-k2 / kc ** 2)), 0.0)
+        dk *= amp
+        inv_k2 = np.where(k2 > 0, 1.0 / k2, 0.0)
+    del amp
+    psi = np.empty((n, n, n, 3), dtype=np.float64)
+    for a, kv in enumerate((kx[None, None, :], ky[None, :, None], kz[:, None, None])):
+        psi[..., a] = np.fft.irfftn(1j * kv * inv_k2 * dk, s=(n, n, n))
+    del dk
+    rms = np.sqrt(np.mean(np.sum(psi ** 2, axis=-1)))
+    spacing = L / n
+    if rms > 0:
+        psi *= (rms_disp * spacing) / rms
+    q1 = (np.arange(n) + 0.5) * spacing
+    pos = psi
+    pos[..., 0] += q1[None, None, :]
+    pos[..., 1] += q1[None, :, None]
+    pos[..., 2] += q1[:, None, None]
+    if infall > 0:
+        _apply_infall(pos, n, L, infall, seed if infall_seed is None else infall_seed)
+    return pos.astype(dtype)
+
+
+def _apply_infall(pos, n, L, count, seed, concentration=10.0):
+    """Spherical infall regions: centres uniform, radii log-uniform in
+    [0.5, 5] lattice spacings, NFW-like radial compression."""
+    rng = np.random.default_rng(seed + 1000003)
+    spacing = L / n
+    centres = rng.uniform(0.0, L, size=(count, 3))
+    radii = np.exp(rng.uniform(np.log(0.5), np.log(5.0), size=count)) * spacing
+    flat = pos.reshape(-1, 3)
+    for c, r in zip(centres, radii):
+        reach = 3.0 * r
+        d = flat - c
+        d -= L * np.round(d / L)
+        dist = np.sqrt(np.sum(d * d, axis=1))
+        sel = dist < reach
+        if not np.any(sel):
+            continue
+        x = dist[sel] / reach
+        # enclosed-mass-like profile: shrink radii toward the centre
+        g = np.log1p(concentration * x) / np.log1p(concentration)
+        new = reach * (x * 0.5 + 0.5 * g * x)
+        scale = np.where(dist[sel] > 0, new / np.maximum(dist[sel], 1e-12), 1.0)
+        flat[sel] = c + d[sel] * scale[:, None]
+
+
+def periodic_ghost_lattice(pos: np.ndarray, L: float) -> np.ndarray:
+    """(n,n,n,3) periodic lattice -> (n+1)^3 lattice whose last plane along
+    each axis is the first plane shifted by +L: its (n)^3 cubes are the n^3
+    periodic cubes, in the reference's non-periodic cube convention."""
+    n = pos.shape[0]
+    out = np.empty((n + 1, n + 1, n + 1, 3), dtype=pos.dtype)
+    out[:n, :n, :n] = pos
+    out[:n, :n, n] = pos[:, :, 0] + np.array([L, 0, 0], dtype=pos.dtype)
+    out[:n, n, :] = out[:n, 0, :] + np.array([0, L, 0], dtype=pos.dtype)
+    out[n, :, :] = out[0, :, :] + np.array([0, 0, L], dtype=pos.dtype)
+    return out
+
+
+def bbox6(pos: np.ndarray):
+    """(xmin, xmax, ymin, ymax, zmin, zmax) of a position array."""
+    p = pos.reshape(-1, 3)
+    mn, mx = p.min(axis=0), p.max(axis=0)
+    return np.array([mn[0], mx[0], mn[1], mx[1], mn[2], mx[2]], dtype=np.float32)
