@@ -1,0 +1,783 @@
+// kernels.cuh -- the deposit kernels.
+//
+// Work decomposition: a deposit is a list of work items; an item pairs one
+// output grid (a GridDesc: an octree leaf block, a zoom box, or the grid of a
+// reference-boundary call) with one vertex block of at most 8^3 vertices
+// (7^3 lattice cubes: a meta-cell of a resident lattice, or a sub-block of a
+// reference-format patch).  A CTA stages the block's vertices in shared
+// memory, culls its cubes against the grid box, and deposits the surviving
+// tets with one warp per 32 tets: the tets' candidate (tet, cell) pairs are
+// flattened across the warp, classified with per-tet plane bounds, easy
+// cells are scattered at once and partial cells go through a per-warp
+// shared-memory queue so that 32 lanes always clip together.
+//
+// Mass is accumulated as 64-bit fixed point (2^shift units per mass unit)
+// with integer atomics: the sum is exact and independent of the order in
+// which tets land, so results are bit-reproducible run to run and the same
+// whether a request runs alone or inside a batch.
+#pragma once
+
+#include "geometry.cuh"
+
+namespace adeco {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kMaxVerts = 512;   // 8^3
+constexpr int kMaxCubes = 343;   // 7^3
+constexpr int kQueue = 64;
+
+struct Item {
+    long long base;  // vertex index of the block origin (lattice) or of the patch origin + offset
+    int grid;        // GridDesc index
+    int nv;          // vertex counts vx | vy<<8 | vz<<16 (each <= 8)
+};
+
+enum SrcKind : int { SRC_LATTICE_F4 = 0, SRC_PATCH_F3 = 1 };
+
+struct DepositParams {
+    const Item *items;
+    int n_items;
+    int src_kind;
+    const GridDesc *grids;
+    const void *src;
+    long long stride_y, stride_z;     // vertex strides of the source
+    int order;                        // ORDER_REF or ORDER_CONFORMING
+    int pad_check;                    // skip cubes with a 666 vertex (patch inputs)
+    unsigned long long *out;          // fixed-point accumulators (mixed path)
+    double *out_d;                    // FP64 grids (plain path)
+    int *counter;                     // persistent work counter
+    unsigned long long *stats;        // kNumStats counters or nullptr
+    int *error;                       // device error flag
+};
+
+enum Stat : int {
+    ST_TETS = 0,         // tets with nonzero volume that meet the grid
+    ST_CAND = 1,         // candidate pairs
+    ST_BBOX = 2,         // pairs passing the AABB test
+    ST_INSIDE = 3,       // TET_INSIDE_CELL pairs
+    ST_CELLIN = 4,       // CELL_INSIDE_TET pairs
+    ST_PARTIAL = 5,      // clipped pairs
+    ST_FP64 = 6,         // pairs decided by the FP64 plane test
+    ST_PIECES = 7,       // leaf pieces whose volume was summed
+    kNumStats = 8
+};
+
+// Per-warp table of up to 32 tets (structure of arrays in shared memory).
+struct WarpTets {
+    float q[12][32];     // vertices in the tet's anchor-cell frame (cell units), rounded
+    float qlo[12][32];   // rounding remainders: q + qlo carries the FP64 vertex
+    float n[4][3][32];   // inward face normals
+    float d[4][32];      // plane offsets: inside <=> n.x - d > 0
+    float pos[4][32];    // sum of positive normal components
+    float neg[4][32];    // sum of negative normal components
+    float tol[4][32];    // FP32 error bound of the plane test
+    float bmin[3][32];   // tet AABB in the anchor frame
+    float bmax[3][32];
+    double factor6[32];  // mass per unit of 6x clipped volume (FP64)
+    int lo[3][32];       // anchor cell (first candidate cell) in grid indices
+    int ex[3][32];       // candidate extents (cells per axis)
+    int scan[33];        // exclusive prefix of candidate counts
+    int tetid[32];       // staged cube * 6 + tet of the slot (FP64 route)
+};
+
+// Tets whose conditioning kappa = (longest edge)^3 / |6V| exceeds this take
+// the FP64 route: FP32 vertices in the cell frame carry ~2^-24 * kappa
+// relative error into every cell fraction, so a flat tet (kappa >> 1) would
+// miss the 1e-5 per-cell bar.  Lattice tets sit near kappa = 5.2.
+constexpr float kKappaFp64 = 32.f;
+
+struct SharedMixed {
+    float4 vert[kMaxVerts];
+    uint16_t cubes[kMaxCubes + 1];
+    int n_cubes;
+    int item;
+    GridDesc g;
+    WarpTets wt[kWarps];
+    uint32_t queue[kWarps][kQueue];
+};
+
+__device__ __forceinline__ void stat_add(unsigned long long *stats, int which, unsigned long long v)
+{
+    if (stats && v) atomicAdd(stats + which, v);
+}
+
+// warp-wide sum of a per-lane count, added once per warp
+__device__ __forceinline__ void warp_stat(unsigned long long *stats, int which, unsigned v)
+{
+    if (!stats) return;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) stat_add(stats, which, v);
+}
+
+// ---------------------------------------------------------------- staging
+__device__ __forceinline__ void stage_block(const DepositParams &P, const Item &it, float4 *vert, int vx, int vy,
+                                            int vz)
+{
+    const int nvt = vx * vy * vz;
+    for (int v = threadIdx.x; v < nvt; v += blockDim.x) {
+        const int i = v % vx, r = v / vx, j = r % vy, k = r / vy;
+        const long long gi = it.base + i + P.stride_y * j + P.stride_z * k;
+        float4 p;
+        if (P.src_kind == SRC_LATTICE_F4) {
+            p = __ldg(reinterpret_cast<const float4 *>(P.src) + gi);
+            p.w = 0.f;
+        } else {
+            const float *s = reinterpret_cast<const float *>(P.src) + 3 * gi;
+            p = make_float4(__ldg(s), __ldg(s + 1), __ldg(s + 2), 0.f);
+            if (P.pad_check) {
+                // the reference's padding test on the float inputs
+                const float sum = __fadd_rn(__fadd_rn(fabsf(__fsub_rn(p.x, 666.f)), fabsf(__fsub_rn(p.y, 666.f))),
+                                            fabsf(__fsub_rn(p.z, 666.f)));
+                if ((double)sum < 1.E-03) p.w = 1.f;
+            }
+        }
+        vert[v] = p;
+    }
+}
+
+// cube (ci,cj,ck) of the staged block: alive if no padding vertex and its AABB
+// strictly overlaps the grid box
+__device__ __forceinline__ bool cube_alive(const float4 *vert, int vx, int vy, int ci, int cj, int ck,
+                                           const GridDesc &g)
+{
+    float mn[3] = {3.4e38f, 3.4e38f, 3.4e38f}, mx[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+    bool pad = false;
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        const float4 p = vert[(ci + (s & 1)) + vx * ((cj + ((s >> 1) & 1)) + vy * (ck + (s >> 2)))];
+        pad |= (p.w != 0.f);
+        mn[0] = fminf(mn[0], p.x); mx[0] = fmaxf(mx[0], p.x);
+        mn[1] = fminf(mn[1], p.y); mx[1] = fmaxf(mx[1], p.y);
+        mn[2] = fminf(mn[2], p.z); mx[2] = fmaxf(mx[2], p.z);
+    }
+    if (pad) return false;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+        if (!(mn[a] < g.gmax[a] && g.gmin[a] < mx[a])) return false;
+    return true;
+}
+
+__device__ __forceinline__ void load_tet(const float4 *vert, int vx, int vy, int cube_local_idx, int t, int order,
+                                         int cvx, int cvy, float3 v[4])
+{
+    const int ci = cube_local_idx % cvx, r = cube_local_idx / cvx, cj = r % cvy, ck = r / cvy;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int3 o = corner_offset(order, tet_conn(t, q));
+        const float4 p = vert[(ci + o.x) + vx * ((cj + o.y) + vy * (ck + o.z))];
+        v[q] = make_float3(p.x, p.y, p.z);
+    }
+}
+
+// ------------------------------------------------------ per-tet set-up
+// Build one tet (bit-exact orientation rule and candidate range), then its
+// FP64 anchor-frame geometry, rounded once to FP32.  Returns the candidate
+// pair count (0 if the tet is skipped).
+// Candidate pairs of one tet are limited to kMaxPairsPerTet so that the
+// per-warp flattened pair index fits 32 bits and a queue entry (5-bit slot,
+// 27-bit local index); a larger tet sets the error flag and is skipped.
+constexpr long long kMaxPairsPerTet = 1LL << 25;
+
+ADECO_HD inline int setup_tet(const float3 vin[4], const GridDesc &g, WarpTets &W, int lane, int *error,
+                              bool *fp64_route)
+{
+    *fp64_route = false;
+    float3 v[4] = {vin[0], vin[1], vin[2], vin[3]};
+    const float v6 = vol6_exact(v[0], v[1], v[2], v[3]);
+    const int sgn = vol6_sign_ref(v6);
+    int lo[3], hi[3];
+    if (!candidate_range(v, g, lo, hi)) return 0;
+    if (sgn == 0) return 0;
+    const long long cnt = (long long)(hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
+    if (cnt > kMaxPairsPerTet) {
+#ifdef __CUDA_ARCH__
+        if (error) atomicOr(error, 1);
+#else
+        if (error) *error |= 1;
+#endif
+        return 0;
+    }
+    if (sgn < 0) { const float3 t = v[0]; v[0] = v[3]; v[3] = t; }
+    // anchor frame: q = (x - (gmin + lo*delta)) * scale, in FP64, rounded to FP32
+    double qd[4][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const double anchor = fma((double)lo[a], g.delta_d[a], g.gmin_d[a]);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const double x = (a == 0) ? (double)v[q].x : ((a == 1) ? (double)v[q].y : (double)v[q].z);
+            qd[q][a] = (x - anchor) * g.scale_d[a];
+        }
+    }
+    float qf[4][3];
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) qf[q][a] = (float)qd[q][a];
+    // |6 V| in the anchor frame, FP64 (the tet's signed-volume normaliser)
+    const double vq6 = fabs(vol6_fast<double>(qd[0], qd[1], qd[2], qd[3]));
+    const double f6 = g.mass_factor / vq6;
+    // planes from the FP32 vertices: inward normals (outward ones negated:
+    // faces (0,1,2) (0,2,3) (0,3,1) (1,3,2) with offsets v0 v0 v0 v1)
+    const int fa[4] = {0, 0, 0, 1}, fb[4] = {2, 3, 1, 2}, fc[4] = {1, 2, 3, 3};
+    float R = 0.f;
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) R = fmaxf(R, fabsf(qf[q][a]));
+    R = fmaxf(R, (float)max(max(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]) + 1.f);
+#pragma unroll
+    for (int f = 0; f < 4; ++f) {
+        // n_in = (vb - va) x (vc - va) with the outward order reversed
+        const float e1x = qf[fb[f]][0] - qf[fa[f]][0], e1y = qf[fb[f]][1] - qf[fa[f]][1],
+                    e1z = qf[fb[f]][2] - qf[fa[f]][2];
+        const float e2x = qf[fc[f]][0] - qf[fa[f]][0], e2y = qf[fc[f]][1] - qf[fa[f]][1],
+                    e2z = qf[fc[f]][2] - qf[fa[f]][2];
+        const float nx = e1y * e2z - e1z * e2y, ny = e1z * e2x - e1x * e2z, nz = e1x * e2y - e1y * e2x;
+        const float dd = nx * qf[fa[f]][0] + ny * qf[fa[f]][1] + nz * qf[fa[f]][2];
+        W.n[f][0][lane] = nx;
+        W.n[f][1][lane] = ny;
+        W.n[f][2][lane] = nz;
+        W.d[f][lane] = dd;
+        W.pos[f][lane] = fmaxf(nx, 0.f) + fmaxf(ny, 0.f) + fmaxf(nz, 0.f);
+        W.neg[f][lane] = fminf(nx, 0.f) + fminf(ny, 0.f) + fminf(nz, 0.f);
+        const float L1 = fmaxf(fmaxf(fabsf(e1x), fabsf(e1y)), fabsf(e1z));
+        const float L2 = fmaxf(fmaxf(fabsf(e2x), fabsf(e2y)), fabsf(e2z));
+        // generous bound on the FP32 rounding of n.x - d (|x| <= R + 1)
+        W.tol[f][lane] = 1.0e-5f * L1 * L2 * (R + 1.f);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            W.q[3 * q + a][lane] = qf[q][a];
+            W.qlo[3 * q + a][lane] = (float)(qd[q][a] - (double)qf[q][a]);
+        }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        W.bmin[a][lane] = fminf(fminf(qf[0][a], qf[1][a]), fminf(qf[2][a], qf[3][a]));
+        W.bmax[a][lane] = fmaxf(fmaxf(qf[0][a], qf[1][a]), fmaxf(qf[2][a], qf[3][a]));
+        W.lo[a][lane] = lo[a];
+        W.ex[a][lane] = hi[a] - lo[a] + 1;
+    }
+    W.factor6[lane] = f6;
+    // conditioning: longest edge cubed over |6V|, both in cell units
+    float L2 = 0.f;
+#pragma unroll
+    for (int a0 = 0; a0 < 4; ++a0)
+#pragma unroll
+        for (int b0 = a0 + 1; b0 < 4; ++b0) {
+            const float dx = qf[a0][0] - qf[b0][0], dy = qf[a0][1] - qf[b0][1], dz = qf[a0][2] - qf[b0][2];
+            L2 = fmaxf(L2, dx * dx + dy * dy + dz * dz);
+        }
+    const float Lm = sqrtf(L2);
+    *fp64_route = !(Lm * Lm * Lm <= kKappaFp64 * (float)vq6);
+    return (int)cnt;
+}
+
+enum PairClass : int { P_NO = 0, P_TET_INSIDE = 1, P_CELL_INSIDE = 2, P_PARTIAL = 3 };
+
+#ifdef __CUDACC__
+// One positively oriented tet, candidate range [lo, hi], deposited by the
+// whole warp in FP64: lanes stride over the candidate cells, each classified
+// with FP64 face planes and, when partial, clipped in FP64.  kFixed selects
+// the output: 64-bit fixed point (mixed path) or FP64 atomics (plain path).
+// Returns the counts of (candidate, partial) pairs seen by this lane.
+template <bool kFixed>
+__device__ void deposit_tet_fp64_warp(const float3 v[4], const int lo[3], const int hi[3], const GridDesc &g,
+                                      unsigned long long *out_fixed, double *out_d, unsigned &n_cand,
+                                      unsigned &n_part)
+{
+    const int lane = threadIdx.x & 31;
+    double qd[4][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const double anchor = fma((double)lo[a], g.delta_d[a], g.gmin_d[a]);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const double x = (a == 0) ? (double)v[q].x : ((a == 1) ? (double)v[q].y : (double)v[q].z);
+            qd[q][a] = (x - anchor) * g.scale_d[a];
+        }
+    }
+    const double vq6 = fabs(vol6_fast<double>(qd[0], qd[1], qd[2], qd[3]));
+    const double f6 = g.mass_factor / vq6;
+    double bmin[3], bmax[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        bmin[a] = fmin(fmin(qd[0][a], qd[1][a]), fmin(qd[2][a], qd[3][a]));
+        bmax[a] = fmax(fmax(qd[0][a], qd[1][a]), fmax(qd[2][a], qd[3][a]));
+    }
+    // inward face planes: faces (0,2,1) (0,3,2) (0,1,3) (1,2,3)
+    double pn[4][3], pd[4], pp[4], pm[4];
+    {
+        const int fa[4] = {0, 0, 0, 1}, fb[4] = {2, 3, 1, 2}, fc[4] = {1, 2, 3, 3};
+#pragma unroll
+        for (int f = 0; f < 4; ++f) {
+            const double e1x = qd[fb[f]][0] - qd[fa[f]][0], e1y = qd[fb[f]][1] - qd[fa[f]][1],
+                         e1z = qd[fb[f]][2] - qd[fa[f]][2];
+            const double e2x = qd[fc[f]][0] - qd[fa[f]][0], e2y = qd[fc[f]][1] - qd[fa[f]][1],
+                         e2z = qd[fc[f]][2] - qd[fa[f]][2];
+            pn[f][0] = e1y * e2z - e1z * e2y;
+            pn[f][1] = e1z * e2x - e1x * e2z;
+            pn[f][2] = e1x * e2y - e1y * e2x;
+            pd[f] = pn[f][0] * qd[fa[f]][0] + pn[f][1] * qd[fa[f]][1] + pn[f][2] * qd[fa[f]][2];
+            pp[f] = fmax(pn[f][0], 0.0) + fmax(pn[f][1], 0.0) + fmax(pn[f][2], 0.0);
+            pm[f] = fmin(pn[f][0], 0.0) + fmin(pn[f][1], 0.0) + fmin(pn[f][2], 0.0);
+        }
+    }
+    const int ex0 = hi[0] - lo[0] + 1, ex1 = hi[1] - lo[1] + 1, ex2 = hi[2] - lo[2] + 1;
+    const long long ncell = (long long)ex0 * ex1 * ex2;
+    for (long long cc = lane; cc < ncell; cc += 32) {
+        const int a = (int)(cc % ex0);
+        const long long rr = cc / ex0;
+        const int b = (int)(rr % ex1), k = (int)(rr / ex1);
+        ++n_cand;
+        // cell origin in the anchor frame (the cell extends 1 along each axis)
+        const double oa = a * g.rcell[0], ob = b * g.rcell[1], ok = k * g.rcell[2];
+        if (!(bmin[0] < oa + 1.0 && oa < bmax[0] && bmin[1] < ob + 1.0 && ob < bmax[1] && bmin[2] < ok + 1.0 &&
+              ok < bmax[2]))
+            continue;
+        bool outside = false, all_in = true;
+#pragma unroll
+        for (int f = 0; f < 4; ++f) {
+            const double base = pn[f][0] * oa + pn[f][1] * ob + pn[f][2] * ok - pd[f];
+            if (base + pp[f] <= 0.0) outside = true;
+            if (!(base + pm[f] > 0.0)) all_in = false;
+        }
+        if (outside) continue;
+        double dm;
+        if (bmin[0] >= oa && bmax[0] <= oa + 1.0 && bmin[1] >= ob && bmax[1] <= ob + 1.0 && bmin[2] >= ok &&
+            bmax[2] <= ok + 1.0) {
+            dm = (double)g.tet_mass;
+        } else if (all_in) {
+            dm = 6.0 * f6;
+        } else {
+            double p[4][3];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                p[q][0] = qd[q][0] - oa;
+                p[q][1] = qd[q][1] - ob;
+                p[q][2] = qd[q][2] - ok;
+            }
+            ++n_part;
+            dm = clip_volume6<double, double>(p) * f6;
+        }
+        if (!(dm > 0.0)) continue;
+        const long long idx =
+            g.out_offset + (lo[0] + a) + (long long)g.dims * ((lo[1] + b) + (long long)g.dims * (lo[2] + k));
+        if (kFixed) {
+            const unsigned long long fx = (unsigned long long)llrint(ldexp(dm, g.shift));
+            if (fx) atomicAdd(out_fixed + idx, fx);
+        } else {
+            atomicAdd(out_d + idx, dm);
+        }
+    }
+}
+#endif
+
+// FP64 evaluation of the four plane bounds for a cell whose FP32 test was
+// inside the error band: exact decision for the FP32-rounded tet.
+ADECO_HD
+#ifdef __CUDA_ARCH__
+__noinline__
+#endif
+int classify_fp64(const WarpTets &W, const GridDesc &g, int s, int a, int b, int c)
+{
+    const double ca = a * g.rcell[0], cb = b * g.rcell[1], cc = c * g.rcell[2];
+    double q[4][3];
+#pragma unroll
+    for (int v = 0; v < 4; ++v)
+#pragma unroll
+        for (int x = 0; x < 3; ++x) q[v][x] = (double)W.q[3 * v + x][s] + (double)W.qlo[3 * v + x][s];
+    const int fa[4] = {0, 0, 0, 1}, fb[4] = {2, 3, 1, 2}, fc[4] = {1, 2, 3, 3};
+    bool all_in = true;
+    for (int f = 0; f < 4; ++f) {
+        const double e1x = q[fb[f]][0] - q[fa[f]][0], e1y = q[fb[f]][1] - q[fa[f]][1], e1z = q[fb[f]][2] - q[fa[f]][2];
+        const double e2x = q[fc[f]][0] - q[fa[f]][0], e2y = q[fc[f]][1] - q[fa[f]][1], e2z = q[fc[f]][2] - q[fa[f]][2];
+        const double nx = e1y * e2z - e1z * e2y, ny = e1z * e2x - e1x * e2z, nz = e1x * e2y - e1y * e2x;
+        const double base = nx * (ca - q[fa[f]][0]) + ny * (cb - q[fa[f]][1]) + nz * (cc - q[fa[f]][2]);
+        const double mx = base + fmax(nx, 0.0) + fmax(ny, 0.0) + fmax(nz, 0.0);
+        const double mn = base + fmin(nx, 0.0) + fmin(ny, 0.0) + fmin(nz, 0.0);
+        if (mx <= 0.0) return P_NO;
+        all_in = all_in && (mn > 0.0);
+    }
+    return all_in ? P_CELL_INSIDE : P_PARTIAL;
+}
+
+ADECO_HD inline int classify_pair(const WarpTets &W, const GridDesc &g, int s, int a, int b, int c, bool &used_fp64)
+{
+    const float fa = (float)a, fb = (float)b, fc = (float)c;
+    // strict AABB overlap with the cell [a,a+1] x [b,b+1] x [c,c+1]
+    if (!(W.bmin[0][s] < fa + 1.f && fa < W.bmax[0][s] && W.bmin[1][s] < fb + 1.f && fb < W.bmax[1][s] &&
+          W.bmin[2][s] < fc + 1.f && fc < W.bmax[2][s]))
+        return P_NO;
+    if (W.bmin[0][s] >= fa && W.bmax[0][s] <= fa + 1.f && W.bmin[1][s] >= fb && W.bmax[1][s] <= fb + 1.f &&
+        W.bmin[2][s] >= fc && W.bmax[2][s] <= fc + 1.f)
+        return P_TET_INSIDE;
+    bool all_in = true, unsure = false;
+#pragma unroll
+    for (int f = 0; f < 4; ++f) {
+        const float base = fmaf(W.n[f][0][s], fa, fmaf(W.n[f][1][s], fb, fmaf(W.n[f][2][s], fc, -W.d[f][s])));
+        const float mx = base + W.pos[f][s];
+        const float mn = base + W.neg[f][s];
+        const float t = W.tol[f][s];
+        if (mx < -t) return P_NO;
+        if (mx <= t) unsure = true;
+        if (mn > t) continue;
+        all_in = false;
+        if (mn > -t) unsure = true;
+    }
+    if (unsure) {
+        used_fp64 = true;
+        return classify_fp64(W, g, s, a, b, c);
+    }
+    return all_in ? P_CELL_INSIDE : P_PARTIAL;
+}
+
+// mass (FP64) of one (tet, cell) pair -> 64-bit fixed point, added to the cell
+__device__ __forceinline__ void scatter(const DepositParams &P, const GridDesc &g, const WarpTets &W, int s, int a,
+                                        int b, int c, double dm)
+{
+    const unsigned long long fx = (unsigned long long)llrint(ldexp(dm, g.shift));
+    if (fx == 0ull) return;
+    const long long i = W.lo[0][s] + a, j = W.lo[1][s] + b, k = W.lo[2][s] + c;
+    const long long idx = g.out_offset + i + (long long)g.dims * (j + (long long)g.dims * k);
+    atomicAdd(P.out + idx, fx);
+}
+
+template <typename Acc>
+__device__ __forceinline__ void clip_and_scatter(const DepositParams &P, const GridDesc &g, const WarpTets &W,
+                                                 uint32_t entry, unsigned &pieces)
+{
+    const int s = entry >> 27;
+    const int local = entry & ((1u << 27) - 1);
+    const int ex0 = W.ex[0][s], ex1 = W.ex[1][s];
+    const int a = local % ex0, r = local / ex0, b = r % ex1, c = r / ex1;
+    float p[4][3];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+        p[v][0] = cell_coord(W.q[3 * v + 0][s], W.qlo[3 * v + 0][s], a, g.drcell[0]);
+        p[v][1] = cell_coord(W.q[3 * v + 1][s], W.qlo[3 * v + 1][s], b, g.drcell[1]);
+        p[v][2] = cell_coord(W.q[3 * v + 2][s], W.qlo[3 * v + 2][s], c, g.drcell[2]);
+    }
+    const Acc v6 = clip_volume6<float, Acc>(p);
+    (void)pieces;
+    const double dm = (double)v6 * W.factor6[s];
+    if (dm > 0.0) scatter(P, g, W, s, a, b, c, dm);
+}
+
+// -------------------------------------------------- mixed batched kernel
+template <typename Acc>
+__global__ void __launch_bounds__(kThreads, 2) deposit_mixed_kernel(DepositParams P)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    SharedMixed &S = *reinterpret_cast<SharedMixed *>(smem_raw);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    WarpTets &W = S.wt[warp];
+    uint32_t *Q = S.queue[warp];
+
+    for (;;) {
+        if (threadIdx.x == 0) {
+            S.item = atomicAdd(P.counter, 1);
+            S.n_cubes = 0;
+        }
+        __syncthreads();
+        const int item = S.item;
+        if (item >= P.n_items) break;
+        const Item it = P.items[item];
+        if (threadIdx.x == 0) S.g = P.grids[it.grid];
+        const int vx = it.nv & 0xff, vy = (it.nv >> 8) & 0xff, vz = (it.nv >> 16) & 0xff;
+        stage_block(P, it, S.vert, vx, vy, vz);
+        __syncthreads();
+        const GridDesc &g = S.g;
+        const int cvx = vx - 1, cvy = vy - 1, cvz = vz - 1;
+        const int ncube = (cvx > 0 && cvy > 0 && cvz > 0) ? cvx * cvy * cvz : 0;
+        for (int c = threadIdx.x; c < ncube; c += blockDim.x) {
+            const int ci = c % cvx, r = c / cvx, cj = r % cvy, ck = r / cvy;
+            if (cube_alive(S.vert, vx, vy, ci, cj, ck, g)) S.cubes[atomicAdd(&S.n_cubes, 1)] = (uint16_t)c;
+        }
+        __syncthreads();
+        const int ntet = 6 * S.n_cubes;
+        unsigned st_tets = 0, st_cand = 0, st_bbox = 0, st_in = 0, st_cin = 0, st_part = 0, st_fp64 = 0, st_pieces = 0;
+        for (int t0 = warp * 32; t0 < ntet; t0 += kThreads) {
+            const int tid = t0 + lane;
+            int cnt = 0;
+            bool route64 = false;
+            if (tid < ntet) {
+                float3 v[4];
+                load_tet(S.vert, vx, vy, S.cubes[tid / 6], tid % 6, P.order, cvx, cvy, v);
+                cnt = setup_tet(v, g, W, lane, P.error, &route64);
+                W.tetid[lane] = tid;
+            }
+            st_tets += (cnt > 0);
+            route64 = route64 && cnt > 0;
+            if (route64) cnt = 0;  // deposited below by the FP64 route
+            unsigned fp64_tets = __ballot_sync(0xffffffffu, route64);
+            // exclusive scan of the candidate counts across the warp
+            int incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            W.scan[lane] = incl - cnt;
+            const int total = __shfl_sync(0xffffffffu, incl, 31);
+            if (lane == 31) W.scan[32] = total;
+            __syncwarp();
+            int head = 0, tail = 0;
+            for (int pb = 0; pb < total; pb += 32) {
+                const int pidx = pb + lane;
+                bool part = false;
+                uint32_t entry = 0;
+                if (pidx < total) {
+                    // owning tet: last slot with scan <= pidx
+                    int s = 0;
+#pragma unroll
+                    for (int step = 16; step > 0; step >>= 1)
+                        if (W.scan[s + step] <= pidx) s += step;
+                    const int local = pidx - W.scan[s];
+                    const int ex0 = W.ex[0][s], ex1 = W.ex[1][s];
+                    const int a = local % ex0, r = local / ex0, b = r % ex1, c = r / ex1;
+                    ++st_cand;
+                    bool f64 = false;
+                    const int cls = classify_pair(W, g, s, a, b, c, f64);
+                    st_fp64 += f64;
+                    if (cls == P_TET_INSIDE) {
+                        ++st_in;
+                        ++st_bbox;
+                        scatter(P, g, W, s, a, b, c, (double)g.tet_mass);
+                    } else if (cls == P_CELL_INSIDE) {
+                        ++st_cin;
+                        ++st_bbox;
+                        scatter(P, g, W, s, a, b, c, 6.0 * W.factor6[s]);
+                    } else if (cls == P_PARTIAL) {
+                        ++st_part;
+                        ++st_bbox;
+                        part = true;
+                        entry = ((uint32_t)s << 27) | (uint32_t)local;
+                    }
+                }
+                const unsigned bal = __ballot_sync(0xffffffffu, part);
+                if (part) Q[(head + __popc(bal & ((1u << lane) - 1))) & (kQueue - 1)] = entry;
+                head += __popc(bal);
+                __syncwarp();
+                if (head - tail >= 32) {
+                    clip_and_scatter<Acc>(P, g, W, Q[(tail + lane) & (kQueue - 1)], st_pieces);
+                    tail += 32;
+                    __syncwarp();
+                }
+            }
+            if (lane < head - tail) clip_and_scatter<Acc>(P, g, W, Q[(tail + lane) & (kQueue - 1)], st_pieces);
+            __syncwarp();
+            // ill-conditioned tets of this group: whole warp, FP64
+            while (fp64_tets) {
+                const int src = __ffs(fp64_tets) - 1;
+                fp64_tets &= fp64_tets - 1;
+                const int tid64 = W.tetid[src];
+                float3 v[4];
+                load_tet(S.vert, vx, vy, S.cubes[tid64 / 6], tid64 % 6, P.order, cvx, cvy, v);
+                if (vol6_sign_ref(vol6_exact(v[0], v[1], v[2], v[3])) < 0) {
+                    const float3 t = v[0];
+                    v[0] = v[3];
+                    v[3] = t;
+                }
+                int lo[3], hi[3];
+                candidate_range(v, g, lo, hi);
+                unsigned c64 = 0, p64 = 0;
+                deposit_tet_fp64_warp<true>(v, lo, hi, g, P.out, nullptr, c64, p64);
+                st_cand += c64;
+                st_part += p64;
+                st_fp64 += c64;
+            }
+            __syncwarp();
+        }
+        if (P.stats) {
+            warp_stat(P.stats, ST_TETS, st_tets);
+            warp_stat(P.stats, ST_CAND, st_cand);
+            warp_stat(P.stats, ST_BBOX, st_bbox);
+            warp_stat(P.stats, ST_INSIDE, st_in);
+            warp_stat(P.stats, ST_CELLIN, st_cin);
+            warp_stat(P.stats, ST_PARTIAL, st_part);
+            warp_stat(P.stats, ST_FP64, st_fp64);
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------ plain FP64 kernel
+// The baseline the batched kernel is measured against: one warp per cube,
+// every tet classified and clipped in FP64 lane-per-cell, FP64 atomics into
+// the output grid; one launch per request.
+__global__ void __launch_bounds__(kThreads) deposit_plain_fp64_kernel(DepositParams P, long long cube_begin,
+                                                                      long long cube_end,
+                                                                      const long long *item_cube_offset)
+{
+    const int lane = threadIdx.x & 31;
+    const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long cube = cube_begin + gw; cube < cube_end; cube += nw) {
+        // item owning this cube (binary search over the cube offsets)
+        int lo_i = 0, hi_i = P.n_items - 1;
+        while (lo_i < hi_i) {
+            const int mid = (lo_i + hi_i + 1) >> 1;
+            if (item_cube_offset[mid] <= cube) lo_i = mid; else hi_i = mid - 1;
+        }
+        const Item it = P.items[lo_i];
+        const GridDesc g = P.grids[it.grid];
+        const int vx = it.nv & 0xff, vy = (it.nv >> 8) & 0xff;
+        const int cvx = vx - 1, cvy = vy - 1;
+        const int c = (int)(cube - item_cube_offset[lo_i]);
+        const int ci = c % cvx, r = c / cvx, cj = r % cvy, ck = r / cvy;
+        float3 corner[8];
+        bool pad = false;
+#pragma unroll
+        for (int s = 0; s < 8; ++s) {
+            const int3 o = corner_offset(P.order, s);
+            const long long gi = it.base + (ci + o.x) + P.stride_y * (cj + o.y) + P.stride_z * (ck + o.z);
+            if (P.src_kind == SRC_LATTICE_F4) {
+                const float4 p = __ldg(reinterpret_cast<const float4 *>(P.src) + gi);
+                corner[s] = make_float3(p.x, p.y, p.z);
+            } else {
+                const float *q = reinterpret_cast<const float *>(P.src) + 3 * gi;
+                corner[s] = make_float3(__ldg(q), __ldg(q + 1), __ldg(q + 2));
+                if (P.pad_check) {
+                    const float sum = __fadd_rn(__fadd_rn(fabsf(__fsub_rn(corner[s].x, 666.f)),
+                                                          fabsf(__fsub_rn(corner[s].y, 666.f))),
+                                                fabsf(__fsub_rn(corner[s].z, 666.f)));
+                    pad |= ((double)sum < 1.E-03);
+                }
+            }
+        }
+        if (pad) continue;
+        for (int t = 0; t < 6; ++t) {
+            float3 v[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) v[q] = corner[tet_conn(t, q)];
+            const float v6 = vol6_exact(v[0], v[1], v[2], v[3]);
+            const int sgn = vol6_sign_ref(v6);
+            int lo[3], hi[3];
+            if (!candidate_range(v, g, lo, hi) || sgn == 0) continue;
+            if (sgn < 0) { const float3 tt = v[0]; v[0] = v[3]; v[3] = tt; }
+            unsigned nc = 0, np = 0;
+            deposit_tet_fp64_warp<false>(v, lo, hi, g, nullptr, P.out_d, nc, np);
+        }
+    }
+}
+
+// ------------------------------------------- parity / diagnostics kernels
+// Per tet of a patch sequence: vertex slots after the orientation rule, the
+// volume sign, in-grid flag and candidate range (13 ints, as the oracle's
+// records); and per cell the number of tets whose candidate range covers it.
+__global__ void tet_records_kernel(const float *patches, int m, long long cube_begin, long long cube_end,
+                                   GridDesc g, int order, int *rec, unsigned int *cand)
+{
+    const long long cube = cube_begin + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (cube >= cube_end) return;
+    const long long cpp = (long long)m * m * m;
+    const long long fpp = 3LL * (m + 1) * (m + 1) * (m + 1);
+    const float *patch = patches + (cube / cpp) * fpp;
+    const int local = (int)(cube % cpp);
+    const int k = local / (m * m), r = local % (m * m), j = r / m, i = r % m;
+    float3 corner[8];
+    for (int s = 0; s < 8; ++s) {
+        const int3 o = corner_offset(order, s);
+        const long long id = (i + o.x) + (long long)(m + 1) * ((j + o.y) + (long long)(m + 1) * (k + o.z));
+        corner[s] = make_float3(patch[3 * id], patch[3 * id + 1], patch[3 * id + 2]);
+    }
+    for (int t = 0; t < 6; ++t) {
+        int *R = rec ? rec + 13 * ((cube - cube_begin) * 6 + t) : nullptr;
+        float3 v[4];
+        int slot[4];
+        for (int q = 0; q < 4; ++q) {
+            slot[q] = tet_conn(t, q);
+            v[q] = corner[slot[q]];
+        }
+        const int sgn = vol6_sign_ref(vol6_exact(v[0], v[1], v[2], v[3]));
+        if (sgn < 0) { const int tmp = slot[0]; slot[0] = slot[3]; slot[3] = tmp; }
+        int lo[3], hi[3];
+        const bool in = candidate_range(v, g, lo, hi);
+        if (R) {
+            for (int q = 0; q < 4; ++q) R[q] = slot[q];
+            R[4] = sgn;
+            R[5] = in ? 1 : 0;
+            for (int a = 0; a < 3; ++a) {
+                R[6 + 2 * a] = in ? lo[a] : -1;
+                R[7 + 2 * a] = in ? hi[a] : -1;
+            }
+            R[12] = 0;
+        }
+        if (cand && in && sgn != 0)
+            for (int z = lo[2]; z <= hi[2]; ++z)
+                for (int y = lo[1]; y <= hi[1]; ++y)
+                    for (int x = lo[0]; x <= hi[0]; ++x)
+                        atomicAdd(cand + x + (long long)g.dims * (y + (long long)g.dims * z), 1u);
+    }
+}
+
+// fixed point -> FP64 mass (and optionally += into an FP32 grid)
+__global__ void fixed_to_f64_kernel(const unsigned long long *in, double *out, long long n, double scale)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = (double)in[i] * scale;
+}
+
+__global__ void fixed_accumulate_f64_kernel(const unsigned long long *in, double *out, long long n, double scale)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] += (double)in[i] * scale;
+}
+
+__global__ void fixed_accumulate_f32_kernel(const unsigned long long *in, float *out, long long n, double scale)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = __fadd_rn(out[i], (float)((double)in[i] * scale));
+}
+
+// per-leaf fixed-point grids -> FP64 with each grid's own scale
+__global__ void fixed_to_f64_grids_kernel(const unsigned long long *in, double *out, const GridDesc *grids,
+                                          int n_grids, long long cells_per_grid)
+{
+    const long long n = (long long)n_grids * cells_per_grid;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int gi = (int)(i / cells_per_grid);
+        out[i] = ldexp((double)in[i], -grids[gi].shift);
+    }
+}
+
+// Meta-cell AABBs of a resident float4 lattice (7^3-cube meta-cells): one
+// warp per meta-cell, min/max over its <= 8^3 vertices.
+__global__ void meta_bbox_kernel(const float4 *pos, int nx, int ny, int nz, int cdx, int cdy, int cdz, float *bbox6)
+{
+    const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const long long nmc = (long long)cdx * cdy * cdz;
+    if (w >= nmc) return;
+    const int cx = (int)(w % cdx), r = (int)(w / cdx), cy = r % cdy, cz = r / cdy;
+    const int ox = cx * 7, oy = cy * 7, oz = cz * 7;
+    const int dx = (cx + 1 == cdx) ? nx - ox : 8, dy = (cy + 1 == cdy) ? ny - oy : 8, dz = (cz + 1 == cdz) ? nz - oz : 8;
+    float mn[3] = {3.4e38f, 3.4e38f, 3.4e38f}, mx[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+    const int nv = dx * dy * dz;
+    for (int v = lane; v < nv; v += 32) {
+        const int i = v % dx, rr = v / dx, j = rr % dy, k = rr / dy;
+        const float4 p = pos[(ox + i) + (long long)nx * ((oy + j) + (long long)ny * (oz + k))];
+        mn[0] = fminf(mn[0], p.x); mx[0] = fmaxf(mx[0], p.x);
+        mn[1] = fminf(mn[1], p.y); mx[1] = fmaxf(mx[1], p.y);
+        mn[2] = fminf(mn[2], p.z); mx[2] = fmaxf(mx[2], p.z);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            mn[a] = fminf(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], o));
+            mx[a] = fmaxf(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], o));
+        }
+    if (lane == 0)
+        for (int a = 0; a < 3; ++a) {
+            bbox6[6 * w + a] = mn[a];
+            bbox6[6 * w + 3 + a] = mx[a];
+        }
+}
+
+}  // namespace adeco

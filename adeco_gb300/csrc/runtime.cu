@@ -1,0 +1,1111 @@
+// runtime.cu -- host runtime and C ABI of libadeco_gb300.so (include/adeco_deposit.h).
+//
+// One process drives one GPU.  The reference boundary (adeco_deposit_tets*)
+// replaces DepositWrapper::deposit_tets / resample() (src/AdDeposit2Grid.cu:229-584):
+// positions are copied to HBM once per call, the deposit runs as one
+// persistent launch over (grid, vertex-block) work items, and the result is
+// added into the caller's grid.  Sessions keep the particle lattice, its
+// meta-cells and the octree resident and run the leaf deposit either as one
+// batched persistent launch (mixed precision) or as one FP64 launch per leaf
+// (the plain baseline).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <climits>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/adeco_deposit.h"
+#include "kernels.cuh"
+#include "octree.h"
+
+using namespace adeco;
+
+// ------------------------------------------------------------- errors
+static thread_local std::string g_last_error;
+
+static int fail(int code, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+#define CUDA_TRY(call)                                                                                   \
+    do {                                                                                                 \
+        cudaError_t e_ = (call);                                                                         \
+        if (e_ != cudaSuccess) return fail(ADECO_ERR_CUDA, "%s failed: %s (%s:%d)", #call,               \
+                                           cudaGetErrorString(e_), __FILE__, __LINE__);                  \
+    } while (0)
+
+extern "C" const char *adeco_last_error(void) { return g_last_error.c_str(); }
+extern "C" int adeco_abi_version(void) { return ADECO_ABI_VERSION; }
+
+// ------------------------------------------------------------- helpers
+namespace {
+
+template <typename T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    ~DevBuf() { release(); }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    int reserve(size_t count)
+    {
+        if (count <= n && p) return ADECO_OK;
+        release();
+        if (count == 0) count = 1;
+        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return fail(e == cudaErrorMemoryAllocation ? ADECO_ERR_MEMORY : ADECO_ERR_CUDA,
+                        "cudaMalloc of %zu bytes failed: %s", count * sizeof(T), cudaGetErrorString(e));
+        }
+        n = count;
+        return ADECO_OK;
+    }
+};
+
+// fixed-point exponent for a grid that at most `tets` tets of mass `mass` touch
+int choose_shift(double tets, double mass)
+{
+    const double bound = std::max(tets * std::max(mass, 1e-30), 1e-30);
+    int s = 62 - (int)std::ceil(std::log2(bound + 1.0));
+    return std::min(52, std::max(8, s));
+}
+
+// The request grid: FP32 fields reproduce the reference's range arithmetic,
+// FP64 fields the FP64 oracle's geometry (cubic cells: scale = 1/dx on all
+// axes, as src/AdDepositTets2Grid.h:569).
+GridDesc make_grid(const float bbox[6], int dims, double tet_mass, int shift, long long out_offset)
+{
+    GridDesc g;
+    std::memset(&g, 0, sizeof g);
+    for (int a = 0; a < 3; ++a) {
+        g.gmin[a] = bbox[2 * a];
+        g.gmax[a] = bbox[2 * a + 1];
+        g.delta[a] = (g.gmax[a] - g.gmin[a]) / (float)dims;
+        g.gmin_d[a] = (double)g.gmin[a];
+        g.delta_d[a] = ((double)g.gmax[a] - (double)g.gmin[a]) / (double)dims;
+    }
+    const double s = 1.0 / g.delta_d[0];
+    for (int a = 0; a < 3; ++a) g.scale_d[a] = s;
+    const double cell_vol = g.delta_d[0] * g.delta_d[1] * g.delta_d[2];
+    g.mass_factor = tet_mass * cell_vol * s * s * s;
+    for (int a = 0; a < 3; ++a) {
+        g.rcell[a] = g.delta_d[a] * g.scale_d[a];
+        g.drcell[a] = (float)(g.rcell[a] - 1.0);
+    }
+    g.tet_mass = (float)tet_mass;
+    g.dims = dims;
+    g.shift = shift;
+    g.out_offset = out_offset;
+    return g;
+}
+
+struct DeviceProps {
+    int sms = 0;
+    int mixed_blocks_per_sm = 0;
+    size_t mixed_smem = 0;
+};
+
+int mixed_setup(int device, DeviceProps &dp)
+{
+    static std::mutex mu;
+    static std::map<int, DeviceProps> cache;
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(device);
+    if (it != cache.end()) {
+        dp = it->second;
+        return ADECO_OK;
+    }
+    cudaDeviceProp prop;
+    CUDA_TRY(cudaGetDeviceProperties(&prop, device));
+    dp.sms = prop.multiProcessorCount;
+    dp.mixed_smem = sizeof(SharedMixed);
+    CUDA_TRY(cudaFuncSetAttribute(deposit_mixed_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)dp.mixed_smem));
+    CUDA_TRY(cudaFuncSetAttribute(deposit_mixed_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)dp.mixed_smem));
+    int nb = 0;
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, deposit_mixed_kernel<double>, kThreads,
+                                                           dp.mixed_smem));
+    dp.mixed_blocks_per_sm = std::max(1, nb);
+    cache[device] = dp;
+    return ADECO_OK;
+}
+
+struct LaunchStats {
+    uint64_t launches = 0;
+};
+
+// One persistent launch of the mixed kernel over `n_items` items.
+int launch_mixed(const DeviceProps &dp, DepositParams P, int acc_fp64, cudaStream_t st)
+{
+    if (P.n_items <= 0) return ADECO_OK;
+    CUDA_TRY(cudaMemsetAsync(P.counter, 0, sizeof(int), st));
+    const int grid = std::max(1, std::min(P.n_items, dp.sms * dp.mixed_blocks_per_sm));
+    if (acc_fp64)
+        deposit_mixed_kernel<double><<<grid, kThreads, dp.mixed_smem, st>>>(P);
+    else
+        deposit_mixed_kernel<float><<<grid, kThreads, dp.mixed_smem, st>>>(P);
+    CUDA_TRY(cudaGetLastError());
+    return ADECO_OK;
+}
+
+// Plain FP64 launch over the cubes of `n_items` items.
+// d_cube_off: n_items+1 cube offsets of the items (device), [c0, c1) their range.
+int launch_plain(const DeviceProps &dp, DepositParams P, const long long *d_cube_off, long long c0, long long c1,
+                 cudaStream_t st)
+{
+    if (P.n_items <= 0 || c1 <= c0) return ADECO_OK;
+    const long long warps = c1 - c0;
+    const long long want = (warps * 32 + kThreads - 1) / kThreads;
+    const int grid = (int)std::max(1LL, std::min(want, (long long)dp.sms * 8));
+    deposit_plain_fp64_kernel<<<grid, kThreads, 0, st>>>(P, c0, c1, d_cube_off);
+    CUDA_TRY(cudaGetLastError());
+    return ADECO_OK;
+}
+
+int select_device(int use_specific_gpu, size_t device_id, int &dev)
+{
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count <= 0)
+        return fail(ADECO_ERR_DEVICE, "no CUDA device available (%s)", cudaGetErrorString(e));
+    if (use_specific_gpu && device_id >= (size_t)count)
+        return fail(ADECO_ERR_DEVICE, "selected invalid device number: %zu of %d devices", device_id, count);
+    dev = use_specific_gpu ? (int)device_id : 0;
+    CUDA_TRY(cudaSetDevice(dev));
+    return ADECO_OK;
+}
+
+// Work items for patches [p0, p0+np) of (m+1)^3-vertex patches: sub-blocks of
+// at most 7^3 cubes each.
+void patch_items(size_t p0, size_t np, int m, int grid, std::vector<Item> &items, std::vector<long long> *cube_off)
+{
+    const long long n1 = m + 1, n2 = n1 * n1;
+    const int nsb = MetaGrid::ceil_div(m, kMetaCubes);
+    long long cubes = cube_off && !cube_off->empty() ? cube_off->back() : 0;
+    for (size_t p = p0; p < p0 + np; ++p) {
+        const long long pbase = (long long)p * n1 * n2;
+        for (int sz = 0; sz < nsb; ++sz)
+            for (int sy = 0; sy < nsb; ++sy)
+                for (int sx = 0; sx < nsb; ++sx) {
+                    const int ox = sx * kMetaCubes, oy = sy * kMetaCubes, oz = sz * kMetaCubes;
+                    const int vx = std::min(kMetaCubes + 1, m + 1 - ox), vy = std::min(kMetaCubes + 1, m + 1 - oy),
+                              vz = std::min(kMetaCubes + 1, m + 1 - oz);
+                    Item it;
+                    it.base = pbase + ox + n1 * oy + n2 * oz;
+                    it.grid = grid;
+                    it.nv = vx | (vy << 8) | (vz << 16);
+                    items.push_back(it);
+                    if (cube_off) {
+                        cube_off->push_back(cubes);
+                        cubes += (long long)(vx - 1) * (vy - 1) * (vz - 1);
+                    }
+                }
+    }
+    if (cube_off) cube_off->push_back(cubes);
+}
+
+int validate_boundary(size_t patch_offset, size_t num_patches, const float *positions, size_t positions_size, int m,
+                      const float *bbox, int dims, const void *data)
+{
+    if (m < 1) return fail(ADECO_ERR_ARGUMENT, "meta_cells_per_patch must be >= 1 (got %d)", m);
+    if (dims < 1) return fail(ADECO_ERR_ARGUMENT, "dims must be >= 1 (got %d)", dims);
+    if (dims > 4096) return fail(ADECO_ERR_LIMIT, "dims %d above the supported 4096", dims);
+    if (!positions || !bbox || !data) return fail(ADECO_ERR_ARGUMENT, "null positions, bbox or data pointer");
+    const size_t fpp = 3 * (size_t)(m + 1) * (m + 1) * (m + 1);
+    const size_t cpp = (size_t)m * m * m;
+    if (num_patches * cpp >= (size_t)INT_MAX)
+        return fail(ADECO_ERR_OVERFLOW, "num_cells will cause integer overflow (%zu patches of %zu cubes)",
+                    num_patches, cpp);
+    if (positions_size % fpp != 0)
+        return fail(ADECO_ERR_ARGUMENT, "positions_size %zu is not a multiple of %zu floats per patch",
+                    positions_size, fpp);
+    if (patch_offset + num_patches > positions_size / fpp)
+        return fail(ADECO_ERR_INCONSISTENT, "inconsistent point array: patches [%zu,%zu) of %zu", patch_offset,
+                    patch_offset + num_patches, positions_size / fpp);
+    for (int a = 0; a < 3; ++a)
+        if (!(bbox[2 * a + 1] > bbox[2 * a]))
+            return fail(ADECO_ERR_ARGUMENT, "bbox axis %d is empty (%g >= %g)", a, bbox[2 * a], bbox[2 * a + 1]);
+    return ADECO_OK;
+}
+
+}  // namespace
+
+// ============================================================ boundary
+// Deposit patches [patch_offset, +num_patches) of device-resident patch data
+// into d_fixed (mixed, fixed point 2^shift) or d_f64 (plain FP64).
+static int deposit_device_core(int dev, const float *d_pos, size_t patch_offset, size_t num_patches, int m,
+                               const float *bbox, int dims, int precision, int order, double tet_mass,
+                               unsigned long long *d_fixed, double *d_f64, int shift, cudaStream_t st)
+{
+    DeviceProps dp;
+    int rc = mixed_setup(dev, dp);
+    if (rc) return rc;
+    std::vector<Item> items;
+    std::vector<long long> cube_off;
+    patch_items(patch_offset, num_patches, m, 0, items, precision == ADECO_PREC_FP64 ? &cube_off : nullptr);
+    GridDesc g = make_grid(bbox, dims, tet_mass, shift, 0);
+    DevBuf<Item> d_items;
+    DevBuf<GridDesc> d_grid;
+    DevBuf<int> d_counter;
+    DevBuf<long long> d_cube_off;
+    if ((rc = d_items.reserve(items.size())) || (rc = d_grid.reserve(1)) || (rc = d_counter.reserve(2))) return rc;
+    CUDA_TRY(cudaMemsetAsync(d_counter.p, 0, 2 * sizeof(int), st));
+    CUDA_TRY(cudaMemcpyAsync(d_items.p, items.data(), items.size() * sizeof(Item), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(d_grid.p, &g, sizeof g, cudaMemcpyHostToDevice, st));
+    DepositParams P;
+    std::memset(&P, 0, sizeof P);
+    P.items = d_items.p;
+    P.n_items = (int)items.size();
+    P.src_kind = SRC_PATCH_F3;
+    P.grids = d_grid.p;
+    P.src = d_pos;
+    P.stride_y = m + 1;
+    P.stride_z = (long long)(m + 1) * (m + 1);
+    P.order = order;
+    P.pad_check = 1;
+    P.out = d_fixed;
+    P.out_d = d_f64;
+    P.counter = d_counter.p;
+    P.error = d_counter.p + 1;
+    if (precision == ADECO_PREC_FP64) {
+        if ((rc = d_cube_off.reserve(cube_off.size()))) return rc;
+        CUDA_TRY(cudaMemcpyAsync(d_cube_off.p, cube_off.data(), cube_off.size() * sizeof(long long),
+                                 cudaMemcpyHostToDevice, st));
+        rc = launch_plain(dp, P, d_cube_off.p, 0, cube_off.back(), st);
+    } else {
+        rc = launch_mixed(dp, P, 1, st);
+    }
+    if (rc) return rc;
+    int err = 0;
+    CUDA_TRY(cudaMemcpyAsync(&err, d_counter.p + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    if (err) return fail(ADECO_ERR_LIMIT, "a tet spans more than 2^25 candidate cells of the grid");
+    return ADECO_OK;
+}
+
+extern "C" int adeco_deposit_tets_ex(const adeco_deposit_args *a)
+{
+    if (!a) return fail(ADECO_ERR_ARGUMENT, "null args");
+    if (a->positions_size == 0 || a->num_patches == 0) return ADECO_OK;  // the reference returns silently
+    int rc = validate_boundary(a->patch_offset, a->num_patches, a->positions, a->positions_size,
+                               a->meta_cells_per_patch, a->bbox, a->dims, a->data);
+    if (rc) return rc;
+    if (a->precision != ADECO_PREC_MIXED && a->precision != ADECO_PREC_FP64)
+        return fail(ADECO_ERR_ARGUMENT, "unknown precision %d", a->precision);
+    if (a->tet_order != ADECO_ORDER_REF && a->tet_order != ADECO_ORDER_CONFORMING)
+        return fail(ADECO_ERR_ARGUMENT, "unknown tet order %d", a->tet_order);
+    if (a->out_type != ADECO_OUT_F32 && a->out_type != ADECO_OUT_F64)
+        return fail(ADECO_ERR_ARGUMENT, "unknown output type %d", a->out_type);
+    int dev = 0;
+    if ((rc = select_device(a->use_specific_gpu, a->device_id, dev))) return rc;
+    const int m = a->meta_cells_per_patch;
+    const size_t fpp = 3 * (size_t)(m + 1) * (m + 1) * (m + 1);
+    const size_t ncell = (size_t)a->dims * a->dims * a->dims;
+    // admission: positions slice + accumulators within 75% of free HBM (the
+    // reference's MAX_GPU_USAGE); larger inputs run in several passes
+    size_t free_b = 0, total_b = 0;
+    CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+    const size_t grid_bytes = ncell * (sizeof(unsigned long long) + sizeof(double));
+    const double budget = 0.75 * (double)free_b;
+    if ((double)grid_bytes >= budget)
+        return fail(ADECO_ERR_MEMORY, "grid too large for device memory (%zu bytes, budget %.0f)", grid_bytes, budget);
+    const size_t patch_bytes = fpp * sizeof(float);
+    size_t per_pass = (size_t)((budget - (double)grid_bytes) / (double)patch_bytes);
+    per_pass = std::max<size_t>(1, std::min(per_pass, a->num_patches));
+
+    cudaStream_t st;
+    CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    DevBuf<float> d_pos;
+    DevBuf<unsigned long long> d_fixed;
+    DevBuf<double> d_f64;
+    rc = d_pos.reserve(per_pass * fpp);
+    if (!rc) rc = (a->precision == ADECO_PREC_FP64) ? d_f64.reserve(ncell) : d_fixed.reserve(ncell);
+    if (!rc && a->precision == ADECO_PREC_FP64) {
+        if (cudaMemsetAsync(d_f64.p, 0, ncell * sizeof(double), st) != cudaSuccess) rc = fail(ADECO_ERR_CUDA, "memset");
+    } else if (!rc) {
+        if (cudaMemsetAsync(d_fixed.p, 0, ncell * sizeof(unsigned long long), st) != cudaSuccess)
+            rc = fail(ADECO_ERR_CUDA, "memset");
+    }
+    // the fixed-point scale is fixed for the whole call
+    const int call_shift = choose_shift(6.0 * (double)a->num_patches * (double)m * m * m, a->tet_mass);
+    for (size_t done = 0; !rc && done < a->num_patches; done += per_pass) {
+        const size_t np = std::min(per_pass, a->num_patches - done);
+        const float *src = a->positions + (a->patch_offset + done) * fpp;
+        if (cudaMemcpyAsync(d_pos.p, src, np * fpp * sizeof(float), cudaMemcpyHostToDevice, st) != cudaSuccess) {
+            rc = fail(ADECO_ERR_CUDA, "H2D positions");
+            break;
+        }
+        // every pass uses the call's shift: deposit patches [0, np) of the slice
+        rc = deposit_device_core(dev, d_pos.p, 0, np, m, a->bbox, a->dims, a->precision, a->tet_order, a->tet_mass,
+                                 d_fixed.p, d_f64.p, call_shift, st);
+    }
+    // convert and add into the caller's grid on the device
+    if (!rc) {
+        const int blocks = 1024;
+        if (a->precision == ADECO_PREC_FP64) {
+            // FP64 plain path accumulated directly in FP64
+        } else {
+            if ((rc = d_f64.reserve(ncell)) == ADECO_OK)
+                fixed_to_f64_kernel<<<blocks, 256, 0, st>>>(d_fixed.p, d_f64.p, (long long)ncell,
+                                                            std::ldexp(1.0, -call_shift));
+        }
+        if (!rc) {
+            std::vector<double> host(ncell);
+            if (cudaMemcpyAsync(host.data(), d_f64.p, ncell * sizeof(double), cudaMemcpyDeviceToHost, st) !=
+                    cudaSuccess ||
+                cudaStreamSynchronize(st) != cudaSuccess) {
+                rc = fail(ADECO_ERR_CUDA, "D2H grid: %s", cudaGetErrorString(cudaGetLastError()));
+            } else if (a->out_type == ADECO_OUT_F64) {
+                double *out = (double *)a->data;
+                for (size_t c = 0; c < ncell; ++c) out[c] += host[c];
+            } else {
+                float *out = (float *)a->data;
+                for (size_t c = 0; c < ncell; ++c) out[c] += (float)host[c];
+            }
+        }
+    }
+    cudaStreamSynchronize(st);
+    cudaStreamDestroy(st);
+    return rc;
+}
+
+extern "C" int adeco_deposit_tets(int use_specific_gpu, size_t device_id, size_t patch_offset, size_t num_patches,
+                                  const float *positions, size_t positions_size, int meta_cells_per_patch,
+                                  const float bbox[6], int dims, float *data)
+{
+    adeco_deposit_args a;
+    std::memset(&a, 0, sizeof a);
+    a.use_specific_gpu = use_specific_gpu;
+    a.device_id = device_id;
+    a.patch_offset = patch_offset;
+    a.num_patches = num_patches;
+    a.positions = positions;
+    a.positions_size = positions_size;
+    a.meta_cells_per_patch = meta_cells_per_patch;
+    a.bbox = bbox;
+    a.dims = dims;
+    a.data = data;
+    a.out_type = ADECO_OUT_F32;
+    a.precision = ADECO_PREC_MIXED;
+    a.tet_order = ADECO_ORDER_REF;
+    a.tet_mass = 1.0;
+    return adeco_deposit_tets_ex(&a);
+}
+
+extern "C" int adeco_deposit_tets_device(const float *d_positions, size_t positions_size, size_t patch_offset,
+                                         size_t num_patches, int m, const float bbox[6], int dims, double *d_out,
+                                         int precision, int tet_order, double tet_mass, void *stream)
+{
+    if (positions_size == 0 || num_patches == 0) return ADECO_OK;
+    int rc = validate_boundary(patch_offset, num_patches, d_positions, positions_size, m, bbox, dims, d_out);
+    if (rc) return rc;
+    int dev = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t ncell = (size_t)dims * dims * dims;
+    const int shift = choose_shift(6.0 * (double)num_patches * (double)m * m * m, tet_mass);
+    if (precision == ADECO_PREC_FP64) {
+        return deposit_device_core(dev, d_positions, patch_offset, num_patches, m, bbox, dims, precision, tet_order,
+                                   tet_mass, nullptr, d_out, shift, st);
+    }
+    DevBuf<unsigned long long> d_fixed;
+    if ((rc = d_fixed.reserve(ncell))) return rc;
+    CUDA_TRY(cudaMemsetAsync(d_fixed.p, 0, ncell * sizeof(unsigned long long), st));
+    rc = deposit_device_core(dev, d_positions, patch_offset, num_patches, m, bbox, dims, precision, tet_order,
+                             tet_mass, d_fixed.p, nullptr, shift, st);
+    if (rc) return rc;
+    fixed_accumulate_f64_kernel<<<1024, 256, 0, st>>>(d_fixed.p, d_out, (long long)ncell, std::ldexp(1.0, -shift));
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return ADECO_OK;
+}
+
+// ============================================================ sessions
+struct adeco_session {
+    int device = 0;
+    int order = ORDER_REF;
+    double tet_mass = 1.0;
+    double hbm_fraction = 0.75;
+    int acc_fp64 = 1;
+    cudaStream_t stream = nullptr;
+    DeviceProps dp;
+    int nx = 0, ny = 0, nz = 0;
+    DevBuf<float4> lattice;
+    MetaGrid meta;
+    float bbox6[6] = {0, 0, 0, 0, 0, 0};  // xmin,xmax,ymin,ymax,zmin,zmax
+    // octree + leaf deposit state
+    Octree tree;
+    bool has_tree = false;
+    int leaf_dims = 16;
+    std::vector<GridDesc> leaf_grids;
+    std::vector<Item> leaf_items;
+    std::vector<std::vector<int>> leaf_item_ranges;
+    DevBuf<Item> d_items;
+    DevBuf<GridDesc> d_grids;
+    DevBuf<unsigned long long> d_fixed;
+    DevBuf<double> d_out;
+    DevBuf<int> d_counter;
+    DevBuf<unsigned long long> d_stats;
+    DevBuf<long long> d_cube_off;
+    std::vector<long long> cube_off;
+    size_t out_values = 0;
+    cudaGraphExec_t graph_exec = nullptr;
+    cudaGraph_t graph = nullptr;
+    std::mutex mu;
+    // batches (serving)
+    struct Batch;
+    std::map<uint64_t, std::shared_ptr<Batch>> batches;
+    uint64_t next_batch = 1;
+};
+
+static void session_drop_graph(adeco_session *s)
+{
+    if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
+    if (s->graph) cudaGraphDestroy(s->graph);
+    s->graph_exec = nullptr;
+    s->graph = nullptr;
+}
+
+__global__ void xyz_to_float4_kernel(const float *xyz, float4 *out, long long n)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = make_float4(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], 0.f);
+}
+
+extern "C" int adeco_session_create(const adeco_session_config *cfg, const float *positions, int nx, int ny, int nz,
+                                    adeco_session **out)
+{
+    if (!out || !positions) return fail(ADECO_ERR_ARGUMENT, "null positions or output pointer");
+    *out = nullptr;
+    if (nx < 2 || ny < 2 || nz < 2) return fail(ADECO_ERR_ARGUMENT, "lattice must be at least 2^3 (got %d,%d,%d)", nx, ny, nz);
+    std::unique_ptr<adeco_session> s(new adeco_session());
+    if (cfg) {
+        s->device = cfg->device;
+        s->order = cfg->tet_order;
+        s->tet_mass = cfg->tet_mass > 0 ? cfg->tet_mass : 1.0;
+        s->hbm_fraction = cfg->hbm_fraction > 0 ? cfg->hbm_fraction : 0.75;
+        s->acc_fp64 = cfg->accumulate_fp64;
+    }
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0) return fail(ADECO_ERR_DEVICE, "no CUDA device");
+    if (s->device < 0 || s->device >= count) return fail(ADECO_ERR_DEVICE, "invalid device %d", s->device);
+    CUDA_TRY(cudaSetDevice(s->device));
+    int rc = mixed_setup(s->device, s->dp);
+    if (rc) return rc;
+    CUDA_TRY(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+    s->nx = nx; s->ny = ny; s->nz = nz;
+    const long long n = (long long)nx * ny * nz;
+    if ((rc = s->lattice.reserve((size_t)n))) return rc;
+    {
+        DevBuf<float> raw;
+        if ((rc = raw.reserve((size_t)n * 3))) return rc;
+        CUDA_TRY(cudaMemcpyAsync(raw.p, positions, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+        xyz_to_float4_kernel<<<std::min<long long>((n + 255) / 256, 65535), 256, 0, s->stream>>>(raw.p, s->lattice.p, n);
+        CUDA_TRY(cudaGetLastError());
+        s->meta.init(nx, ny, nz);
+        const long long nmc = (long long)s->meta.count();
+        DevBuf<float> d_bb;
+        if ((rc = d_bb.reserve((size_t)nmc * 6))) return rc;
+        meta_bbox_kernel<<<(unsigned)((nmc * 32 + 255) / 256), 256, 0, s->stream>>>(
+            s->lattice.p, nx, ny, nz, s->meta.cd[0], s->meta.cd[1], s->meta.cd[2], d_bb.p);
+        CUDA_TRY(cudaGetLastError());
+        s->meta.bbox.resize((size_t)nmc * 6);
+        CUDA_TRY(cudaMemcpyAsync(s->meta.bbox.data(), d_bb.p, (size_t)nmc * 6 * sizeof(float), cudaMemcpyDeviceToHost,
+                                 s->stream));
+        CUDA_TRY(cudaStreamSynchronize(s->stream));
+    }
+    float mn[3] = {3.4e38f, 3.4e38f, 3.4e38f}, mx[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+    for (size_t i = 0; i < s->meta.count(); ++i)
+        for (int a = 0; a < 3; ++a) {
+            mn[a] = std::min(mn[a], s->meta.bbox[6 * i + a]);
+            mx[a] = std::max(mx[a], s->meta.bbox[6 * i + 3 + a]);
+        }
+    for (int a = 0; a < 3; ++a) {
+        s->bbox6[2 * a] = mn[a];
+        s->bbox6[2 * a + 1] = mx[a];
+    }
+    if ((rc = s->d_counter.reserve(2)) || (rc = s->d_stats.reserve(kNumStats))) return rc;
+    CUDA_TRY(cudaMemset(s->d_counter.p, 0, 2 * sizeof(int)));
+    *out = s.release();
+    return ADECO_OK;
+}
+
+extern "C" int adeco_session_destroy(adeco_session *s)
+{
+    if (!s) return ADECO_OK;
+    cudaSetDevice(s->device);
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    session_drop_graph(s);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+    return ADECO_OK;
+}
+
+extern "C" int adeco_session_bbox(adeco_session *s, float bbox[6])
+{
+    if (!s || !bbox) return fail(ADECO_ERR_ARGUMENT, "null argument");
+    std::memcpy(bbox, s->bbox6, sizeof(s->bbox6));
+    return ADECO_OK;
+}
+
+extern "C" int adeco_session_build_octree(adeco_session *s, const float *box6, const float *roi6,
+                                          uint64_t max_tets_per_node, int max_level, int leaf_dims)
+{
+    if (!s) return fail(ADECO_ERR_ARGUMENT, "null session");
+    if (leaf_dims < 1 || leaf_dims > 256) return fail(ADECO_ERR_ARGUMENT, "leaf_dims %d out of [1,256]", leaf_dims);
+    if (max_level < 0) return fail(ADECO_ERR_ARGUMENT, "max_level must be >= 0");
+    float box[6];
+    if (box6) {
+        std::memcpy(box, box6, sizeof box);
+    } else {
+        for (int a = 0; a < 3; ++a) {
+            box[a] = s->bbox6[2 * a];
+            box[3 + a] = s->bbox6[2 * a + 1];
+        }
+    }
+    std::lock_guard<std::mutex> lk(s->mu);
+    session_drop_graph(s);
+    s->has_tree = false;
+    // max_tets_per_node = min(global tets / ranks, parameter) (src/AdDepositWorkFlow.h:169), one rank
+    const uint64_t total_tets = 6ull * (uint64_t)(s->nx - 1) * (uint64_t)(s->ny - 1) * (uint64_t)(s->nz - 1);
+    const uint64_t max_tets = std::min(total_tets, max_tets_per_node);
+    if (!s->tree.build(s->meta, box, roi6, max_tets, max_level))
+        return fail(ADECO_ERR_LIMIT, "octree generation did not terminate");
+    s->leaf_dims = leaf_dims;
+    // per-leaf grids and work items (leaf x meta-cell)
+    const size_t nl = s->tree.leaves.size();
+    const long long cells = (long long)leaf_dims * leaf_dims * leaf_dims;
+    s->leaf_grids.resize(nl);
+    s->leaf_items.clear();
+    s->cube_off.clear();
+    long long cubes = 0;
+    for (size_t q = 0; q < nl; ++q) {
+        const OctNode &nd = s->tree.nodes[s->tree.leaves[q]];
+        const float bb[6] = {nd.min[0], nd.min[0] + nd.ext, nd.min[1], nd.min[1] + nd.ext, nd.min[2], nd.min[2] + nd.ext};
+        const int64_t m0 = s->tree.leaf_meta_off[q], m1 = s->tree.leaf_meta_off[q + 1];
+        const int shift = choose_shift(2058.0 * (double)std::max<int64_t>(1, m1 - m0), s->tet_mass);
+        s->leaf_grids[q] = make_grid(bb, leaf_dims, s->tet_mass, shift, (long long)q * cells);
+        for (int64_t k = m0; k < m1; ++k) {
+            int org[3], nv[3];
+            s->meta.range(s->tree.leaf_meta_ids[k], org, nv);
+            Item it;
+            it.base = org[0] + (long long)s->nx * (org[1] + (long long)s->ny * org[2]);
+            it.grid = (int)q;
+            it.nv = nv[0] | (nv[1] << 8) | (nv[2] << 16);
+            s->leaf_items.push_back(it);
+            s->cube_off.push_back(cubes);
+            cubes += (long long)(nv[0] - 1) * (nv[1] - 1) * (nv[2] - 1);
+        }
+    }
+    s->cube_off.push_back(cubes);
+    int rc;
+    s->out_values = nl * (size_t)cells;
+    if ((rc = s->d_items.reserve(s->leaf_items.size())) || (rc = s->d_grids.reserve(nl)) ||
+        (rc = s->d_fixed.reserve(s->out_values)) || (rc = s->d_out.reserve(s->out_values)) ||
+        (rc = s->d_cube_off.reserve(s->cube_off.size())))
+        return rc;
+    CUDA_TRY(cudaMemcpyAsync(s->d_items.p, s->leaf_items.data(), s->leaf_items.size() * sizeof(Item),
+                             cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(cudaMemcpyAsync(s->d_grids.p, s->leaf_grids.data(), nl * sizeof(GridDesc), cudaMemcpyHostToDevice,
+                             s->stream));
+    CUDA_TRY(cudaMemcpyAsync(s->d_cube_off.p, s->cube_off.data(), s->cube_off.size() * sizeof(long long),
+                             cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    s->has_tree = true;
+    return ADECO_OK;
+}
+
+extern "C" int adeco_session_octree_size(adeco_session *s, int *n_nodes, int *n_leaves, int *n_levels)
+{
+    if (!s) return fail(ADECO_ERR_ARGUMENT, "null session");
+    if (!s->has_tree) return fail(ADECO_ERR_STATE, "no octree built");
+    if (n_nodes) *n_nodes = (int)s->tree.nodes.size();
+    if (n_leaves) *n_leaves = (int)s->tree.leaves.size();
+    if (n_levels) *n_levels = s->tree.levels;
+    return ADECO_OK;
+}
+
+extern "C" int adeco_session_octree_nodes(adeco_session *s, adeco_node *nodes, int capacity)
+{
+    if (!s || !nodes) return fail(ADECO_ERR_ARGUMENT, "null argument");
+    if (!s->has_tree) return fail(ADECO_ERR_STATE, "no octree built");
+    if (capacity < (int)s->tree.nodes.size()) return fail(ADECO_ERR_ARGUMENT, "capacity too small");
+    std::vector<int> nmeta(s->tree.nodes.size(), 0);
+    for (size_t q = 0; q < s->tree.leaves.size(); ++q)
+        nmeta[s->tree.leaves[q]] = (int)(s->tree.leaf_meta_off[q + 1] - s->tree.leaf_meta_off[q]);
+    for (size_t i = 0; i < s->tree.nodes.size(); ++i) {
+        const OctNode &n = s->tree.nodes[i];
+        adeco_node &o = nodes[i];
+        o.min[0] = n.min[0]; o.min[1] = n.min[1]; o.min[2] = n.min[2];
+        o.ext = n.ext;
+        o.level = n.level;
+        o.parent = n.parent;
+        o.first_child = n.first_child;
+        o.n_meta = nmeta[i];
+        o.estimate = n.estimate;
+    }
+    return ADECO_OK;
+}
+
+extern "C" int adeco_session_leaves(adeco_session *s, int32_t *leaf_ids, int capacity)
+{
+    if (!s || !leaf_ids) return fail(ADECO_ERR_ARGUMENT, "null argument");
+    if (!s->has_tree) return fail(ADECO_ERR_STATE, "no octree built");
+    if (capacity < (int)s->tree.leaves.size()) return fail(ADECO_ERR_ARGUMENT, "capacity too small");
+    std::copy(s->tree.leaves.begin(), s->tree.leaves.end(), leaf_ids);
+    return ADECO_OK;
+}
+
+extern "C" int adeco_session_leaf_meta(adeco_session *s, int leaf_index, uint64_t *ids, int capacity, int *count)
+{
+    if (!s || !count) return fail(ADECO_ERR_ARGUMENT, "null argument");
+    if (!s->has_tree) return fail(ADECO_ERR_STATE, "no octree built");
+    if (leaf_index < 0 || leaf_index >= (int)s->tree.leaves.size()) return fail(ADECO_ERR_ARGUMENT, "bad leaf index");
+    const int64_t a = s->tree.leaf_meta_off[leaf_index], b = s->tree.leaf_meta_off[leaf_index + 1];
+    *count = (int)(b - a);
+    if (ids) {
+        if (capacity < *count) return fail(ADECO_ERR_ARGUMENT, "capacity too small");
+        std::copy(s->tree.leaf_meta_ids.begin() + a, s->tree.leaf_meta_ids.begin() + b, ids);
+    }
+    return ADECO_OK;
+}
+
+static DepositParams session_params(adeco_session *s, bool stats)
+{
+    DepositParams P;
+    std::memset(&P, 0, sizeof P);
+    P.items = s->d_items.p;
+    P.n_items = (int)s->leaf_items.size();
+    P.src_kind = SRC_LATTICE_F4;
+    P.grids = s->d_grids.p;
+    P.src = s->lattice.p;
+    P.stride_y = s->nx;
+    P.stride_z = (long long)s->nx * s->ny;
+    P.order = s->order;
+    P.pad_check = 0;
+    P.out = s->d_fixed.p;
+    P.out_d = s->d_out.p;
+    P.counter = s->d_counter.p;
+    P.error = s->d_counter.p + 1;
+    P.stats = stats ? s->d_stats.p : nullptr;
+    return P;
+}
+
+// enqueue the batched leaf deposit (memset, persistent kernel, conversion)
+static int enqueue_leaves_mixed(adeco_session *s, bool stats)
+{
+    const size_t nv = s->out_values;
+    CUDA_TRY(cudaMemsetAsync(s->d_fixed.p, 0, nv * sizeof(unsigned long long), s->stream));
+    int rc = launch_mixed(s->dp, session_params(s, stats), s->acc_fp64, s->stream);
+    if (rc) return rc;
+    const long long cells = (long long)s->leaf_dims * s->leaf_dims * s->leaf_dims;
+    fixed_to_f64_grids_kernel<<<s->dp.sms * 4, 256, 0, s->stream>>>(s->d_fixed.p, s->d_out.p, s->d_grids.p,
+                                                                    (int)s->leaf_grids.size(), cells);
+    CUDA_TRY(cudaGetLastError());
+    return ADECO_OK;
+}
+
+extern "C" int adeco_session_deposit_leaves(adeco_session *s, int precision, double *host_out, int collect_stats,
+                                            adeco_timing *timing)
+{
+    if (!s) return fail(ADECO_ERR_ARGUMENT, "null session");
+    if (!s->has_tree) return fail(ADECO_ERR_STATE, "no octree built");
+    std::lock_guard<std::mutex> lk(s->mu);
+    CUDA_TRY(cudaSetDevice(s->device));
+    cudaEvent_t e0, e1, e2;
+    CUDA_TRY(cudaEventCreate(&e0));
+    CUDA_TRY(cudaEventCreate(&e1));
+    CUDA_TRY(cudaEventCreate(&e2));
+    if (collect_stats) CUDA_TRY(cudaMemsetAsync(s->d_stats.p, 0, kNumStats * sizeof(unsigned long long), s->stream));
+    uint64_t launches = 0;
+    int rc = ADECO_OK;
+    if (precision == ADECO_PREC_FP64) {
+        const size_t nv = s->out_values;
+        CUDA_TRY(cudaMemsetAsync(s->d_out.p, 0, nv * sizeof(double), s->stream));
+        CUDA_TRY(cudaEventRecord(e0, s->stream));
+        // one launch per leaf (one request per launch)
+        DepositParams P = session_params(s, false);
+        size_t item0 = 0;
+        for (size_t q = 0; q < s->leaf_grids.size() && !rc; ++q) {
+            size_t item1 = item0;
+            while (item1 < s->leaf_items.size() && s->leaf_items[item1].grid == (int)q) ++item1;
+            DepositParams Q = P;
+            Q.items = s->d_items.p + item0;
+            Q.n_items = (int)(item1 - item0);
+            const long long c0 = s->cube_off[item0], c1 = s->cube_off[item1];
+            if (Q.n_items > 0 && c1 > c0) {
+                rc = launch_plain(s->dp, Q, s->d_cube_off.p + item0, c0, c1, s->stream);
+                ++launches;
+            }
+            item0 = item1;
+        }
+        CUDA_TRY(cudaEventRecord(e1, s->stream));
+        CUDA_TRY(cudaEventRecord(e2, s->stream));
+    } else {
+        CUDA_TRY(cudaMemsetAsync(s->d_fixed.p, 0, s->out_values * sizeof(unsigned long long), s->stream));
+        CUDA_TRY(cudaEventRecord(e0, s->stream));
+        rc = launch_mixed(s->dp, session_params(s, collect_stats != 0), s->acc_fp64, s->stream);
+        launches = 1;
+        CUDA_TRY(cudaEventRecord(e1, s->stream));
+        const long long cells = (long long)s->leaf_dims * s->leaf_dims * s->leaf_dims;
+        fixed_to_f64_grids_kernel<<<s->dp.sms * 4, 256, 0, s->stream>>>(s->d_fixed.p, s->d_out.p, s->d_grids.p,
+                                                                        (int)s->leaf_grids.size(), cells);
+        ++launches;
+        CUDA_TRY(cudaGetLastError());
+        CUDA_TRY(cudaEventRecord(e2, s->stream));
+    }
+    if (rc) return rc;
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    int err = 0;
+    CUDA_TRY(cudaMemcpy(&err, s->d_counter.p + 1, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) {
+        cudaMemset(s->d_counter.p + 1, 0, sizeof(int));
+        return fail(ADECO_ERR_LIMIT, "a tet spans more than 2^25 candidate cells of a leaf grid");
+    }
+    float k_ms = 0.f, t_ms = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&k_ms, e0, e1));
+    CUDA_TRY(cudaEventElapsedTime(&t_ms, e0, e2));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaEventDestroy(e2);
+    if (timing) {
+        std::memset(timing, 0, sizeof *timing);
+        timing->kernel_ms = k_ms;
+        timing->total_ms = t_ms;
+        timing->launches = launches;
+        timing->items = s->leaf_items.size();
+        if (collect_stats) {
+            unsigned long long st[kNumStats];
+            CUDA_TRY(cudaMemcpy(st, s->d_stats.p, sizeof st, cudaMemcpyDeviceToHost));
+            timing->tets = st[ST_TETS];
+            timing->candidate_pairs = st[ST_CAND];
+            timing->partial_pairs = st[ST_PARTIAL];
+            timing->cell_inside_pairs = st[ST_CELLIN];
+            timing->tet_inside_pairs = st[ST_INSIDE];
+            timing->fp64_pairs = st[ST_FP64];
+        }
+    }
+    if (host_out) CUDA_TRY(cudaMemcpy(host_out, s->d_out.p, s->out_values * sizeof(double), cudaMemcpyDeviceToHost));
+    return ADECO_OK;
+}
+
+extern "C" int adeco_session_leaf_grids_device(adeco_session *s, const double **d_grids, size_t *n_values)
+{
+    if (!s || !d_grids || !n_values) return fail(ADECO_ERR_ARGUMENT, "null argument");
+    if (!s->has_tree) return fail(ADECO_ERR_STATE, "no octree built");
+    *d_grids = s->d_out.p;
+    *n_values = s->out_values;
+    return ADECO_OK;
+}
+
+extern "C" int adeco_session_replay_leaves(adeco_session *s, int reps, adeco_timing *timing)
+{
+    if (!s) return fail(ADECO_ERR_ARGUMENT, "null session");
+    if (!s->has_tree) return fail(ADECO_ERR_STATE, "no octree built");
+    if (reps < 1) return fail(ADECO_ERR_ARGUMENT, "reps must be >= 1");
+    std::lock_guard<std::mutex> lk(s->mu);
+    CUDA_TRY(cudaSetDevice(s->device));
+    if (!s->graph_exec) {
+        CUDA_TRY(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = enqueue_leaves_mixed(s, false);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (e != cudaSuccess) return fail(ADECO_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+        s->graph = g;
+        CUDA_TRY(cudaGraphInstantiate(&s->graph_exec, s->graph, 0));
+    }
+    cudaEvent_t e0, e1;
+    CUDA_TRY(cudaEventCreate(&e0));
+    CUDA_TRY(cudaEventCreate(&e1));
+    CUDA_TRY(cudaEventRecord(e0, s->stream));
+    for (int r = 0; r < reps; ++r) CUDA_TRY(cudaGraphLaunch(s->graph_exec, s->stream));
+    CUDA_TRY(cudaEventRecord(e1, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    float ms = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (timing) {
+        std::memset(timing, 0, sizeof *timing);
+        timing->kernel_ms = ms / reps;
+        timing->total_ms = ms / reps;
+        timing->launches = 2ull * reps;
+        timing->items = s->leaf_items.size();
+    }
+    return ADECO_OK;
+}
+
+// ============================================================ diagnostics
+extern "C" int adeco_debug_tet_records(const float *positions, size_t positions_size, int m, size_t cube_begin,
+                                       size_t cube_end, const float bbox[6], int dims, int tet_order, int32_t *records,
+                                       uint32_t *cand)
+{
+    if (!positions || !bbox || m < 1 || dims < 1) return fail(ADECO_ERR_ARGUMENT, "bad arguments");
+    const size_t fpp = 3 * (size_t)(m + 1) * (m + 1) * (m + 1);
+    if (positions_size % fpp) return fail(ADECO_ERR_ARGUMENT, "positions_size not a multiple of the patch size");
+    const size_t cubes_total = positions_size / fpp * (size_t)m * m * m;
+    if (cube_end > cubes_total || cube_begin > cube_end) return fail(ADECO_ERR_ARGUMENT, "cube range out of bounds");
+    int dev = 0;
+    int rc = select_device(0, 0, dev);
+    if (rc) return rc;
+    const size_t ncube = cube_end - cube_begin;
+    const size_t ncell = (size_t)dims * dims * dims;
+    DevBuf<float> d_pos;
+    DevBuf<int> d_rec;
+    DevBuf<unsigned int> d_cand;
+    if ((rc = d_pos.reserve(positions_size)) || (rc = d_rec.reserve(std::max<size_t>(1, ncube * 6 * 13))) ||
+        (rc = d_cand.reserve(ncell)))
+        return rc;
+    CUDA_TRY(cudaMemcpy(d_pos.p, positions, positions_size * sizeof(float), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemset(d_cand.p, 0, ncell * sizeof(unsigned int)));
+    const GridDesc g = make_grid(bbox, dims, 1.0, 32, 0);
+    if (ncube) {
+        tet_records_kernel<<<(unsigned)((ncube + 127) / 128), 128>>>(d_pos.p, m, (long long)cube_begin,
+                                                                     (long long)cube_end, g, tet_order, d_rec.p,
+                                                                     cand ? d_cand.p : nullptr);
+        CUDA_TRY(cudaGetLastError());
+    }
+    CUDA_TRY(cudaDeviceSynchronize());
+    if (records && ncube) CUDA_TRY(cudaMemcpy(records, d_rec.p, ncube * 6 * 13 * sizeof(int), cudaMemcpyDeviceToHost));
+    if (cand) CUDA_TRY(cudaMemcpy(cand, d_cand.p, ncell * sizeof(unsigned int), cudaMemcpyDeviceToHost));
+    return ADECO_OK;
+}
+
+// ============================================================ zoom batches
+// A batch of zoom requests: each request is a cubic box and a resolution; its
+// work items pair the request grid with every meta-cell whose AABB strictly
+// meets the box.  A batch is one persistent launch on its own stream, so
+// batches submitted while others run overlap on the device.
+struct adeco_session::Batch {
+    std::vector<adeco_request> reqs;
+    std::vector<GridDesc> grids;
+    std::vector<long long> offsets;  // first cell of each request
+    size_t cells = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    DevBuf<Item> d_items;
+    DevBuf<GridDesc> d_grids;
+    DevBuf<unsigned long long> d_fixed;
+    DevBuf<int> d_counter;
+    std::chrono::steady_clock::time_point t_submit;
+    double latency_ms = -1.0;
+    int n_items = 0;
+    ~Batch()
+    {
+        if (done) cudaEventDestroy(done);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+static void request_box(const adeco_request &r, float bb[6])
+{
+    const float h = 0.5f * r.side;
+    for (int a = 0; a < 3; ++a) {
+        bb[2 * a] = r.center[a] - h;
+        bb[2 * a + 1] = r.center[a] + h;
+    }
+}
+
+extern "C" int adeco_session_submit(adeco_session *s, const adeco_request *reqs, int n, uint64_t *batch_id)
+{
+    if (!s || !reqs || n <= 0 || !batch_id) return fail(ADECO_ERR_ARGUMENT, "bad arguments");
+    for (int i = 0; i < n; ++i) {
+        if (reqs[i].dims < 1 || reqs[i].dims > 1024) return fail(ADECO_ERR_ARGUMENT, "request %d: dims out of [1,1024]", i);
+        if (!(reqs[i].side > 0.f)) return fail(ADECO_ERR_ARGUMENT, "request %d: side must be > 0", i);
+        if (reqs[i].precision != ADECO_PREC_MIXED) return fail(ADECO_ERR_ARGUMENT, "request %d: batches run the mixed path", i);
+    }
+    CUDA_TRY(cudaSetDevice(s->device));
+    auto b = std::make_shared<adeco_session::Batch>();
+    b->t_submit = std::chrono::steady_clock::now();
+    b->reqs.assign(reqs, reqs + n);
+    std::vector<Item> items;
+    long long off = 0;
+    for (int i = 0; i < n; ++i) {
+        float bb[6];
+        request_box(reqs[i], bb);
+        const float box6[6] = {bb[0], bb[2], bb[4], bb[1], bb[3], bb[5]};
+        const int grid_index = i;
+        size_t first = items.size();
+        for (uint64_t id = 0; id < s->meta.count(); ++id) {
+            const float *m = &s->meta.bbox[6 * id];
+            if (!(m[0] < box6[3] && box6[0] < m[3] && m[1] < box6[4] && box6[1] < m[4] && m[2] < box6[5] &&
+                  box6[2] < m[5]))
+                continue;
+            int org[3], nv[3];
+            s->meta.range(id, org, nv);
+            Item it;
+            it.base = org[0] + (long long)s->nx * (org[1] + (long long)s->ny * org[2]);
+            it.grid = grid_index;
+            it.nv = nv[0] | (nv[1] << 8) | (nv[2] << 16);
+            items.push_back(it);
+        }
+        const double tets = 2058.0 * (double)std::max<size_t>(1, items.size() - first);
+        b->grids.push_back(make_grid(bb, reqs[i].dims, s->tet_mass, choose_shift(tets, s->tet_mass), off));
+        b->offsets.push_back(off);
+        off += (long long)reqs[i].dims * reqs[i].dims * reqs[i].dims;
+    }
+    b->cells = (size_t)off;
+    b->n_items = (int)items.size();
+    // admission by free HBM
+    size_t free_b = 0, total_b = 0;
+    CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+    const double need = (double)b->cells * 8.0 + (double)items.size() * sizeof(Item) + 4096.0;
+    if (need > s->hbm_fraction * (double)free_b)
+        return fail(ADECO_ERR_MEMORY, "batch needs %.0f bytes, admission budget %.0f", need,
+                    s->hbm_fraction * (double)free_b);
+    int rc;
+    if ((rc = b->d_items.reserve(items.size())) || (rc = b->d_grids.reserve(b->grids.size())) ||
+        (rc = b->d_fixed.reserve(b->cells)) || (rc = b->d_counter.reserve(2)))
+        return rc;
+    CUDA_TRY(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    CUDA_TRY(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming));
+    CUDA_TRY(cudaMemcpyAsync(b->d_items.p, items.data(), items.size() * sizeof(Item), cudaMemcpyHostToDevice, b->stream));
+    CUDA_TRY(cudaMemcpyAsync(b->d_grids.p, b->grids.data(), b->grids.size() * sizeof(GridDesc), cudaMemcpyHostToDevice,
+                             b->stream));
+    CUDA_TRY(cudaMemsetAsync(b->d_fixed.p, 0, b->cells * sizeof(unsigned long long), b->stream));
+    CUDA_TRY(cudaMemsetAsync(b->d_counter.p, 0, 2 * sizeof(int), b->stream));
+    DepositParams P;
+    std::memset(&P, 0, sizeof P);
+    P.items = b->d_items.p;
+    P.n_items = b->n_items;
+    P.src_kind = SRC_LATTICE_F4;
+    P.grids = b->d_grids.p;
+    P.src = s->lattice.p;
+    P.stride_y = s->nx;
+    P.stride_z = (long long)s->nx * s->ny;
+    P.order = s->order;
+    P.out = b->d_fixed.p;
+    P.counter = b->d_counter.p;
+    P.error = b->d_counter.p + 1;
+    if ((rc = launch_mixed(s->dp, P, s->acc_fp64, b->stream))) return rc;
+    CUDA_TRY(cudaEventRecord(b->done, b->stream));
+    std::lock_guard<std::mutex> lk(s->mu);
+    *batch_id = s->next_batch++;
+    s->batches[*batch_id] = b;
+    return ADECO_OK;
+}
+
+static std::shared_ptr<adeco_session::Batch> find_batch(adeco_session *s, uint64_t id)
+{
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->batches.find(id);
+    return it == s->batches.end() ? nullptr : it->second;
+}
+
+static void mark_done(adeco_session::Batch &b)
+{
+    if (b.latency_ms < 0)
+        b.latency_ms =
+            std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - b.t_submit).count();
+}
+
+extern "C" int adeco_session_poll(adeco_session *s, uint64_t batch_id, int *done)
+{
+    if (!s || !done) return fail(ADECO_ERR_ARGUMENT, "null argument");
+    auto b = find_batch(s, batch_id);
+    if (!b) return fail(ADECO_ERR_NOT_FOUND, "unknown batch %llu", (unsigned long long)batch_id);
+    const cudaError_t e = cudaEventQuery(b->done);
+    if (e == cudaSuccess) {
+        mark_done(*b);
+        *done = 1;
+        return ADECO_OK;
+    }
+    if (e == cudaErrorNotReady) {
+        *done = 0;
+        return ADECO_OK;
+    }
+    return fail(ADECO_ERR_CUDA, "batch %llu failed: %s", (unsigned long long)batch_id, cudaGetErrorString(e));
+}
+
+extern "C" int adeco_session_wait(adeco_session *s, uint64_t batch_id, double timeout_s)
+{
+    if (!s) return fail(ADECO_ERR_ARGUMENT, "null session");
+    auto b = find_batch(s, batch_id);
+    if (!b) return fail(ADECO_ERR_NOT_FOUND, "unknown batch %llu", (unsigned long long)batch_id);
+    const auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        const cudaError_t e = cudaEventQuery(b->done);
+        if (e == cudaSuccess) {
+            mark_done(*b);
+            return ADECO_OK;
+        }
+        if (e != cudaErrorNotReady) return fail(ADECO_ERR_CUDA, "batch failed: %s", cudaGetErrorString(e));
+        if (std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() > timeout_s)
+            return fail(ADECO_ERR_STATE, "timed out after %.1f s waiting for batch %llu", timeout_s,
+                        (unsigned long long)batch_id);
+        std::this_thread::yield();
+    }
+}
+
+extern "C" int adeco_session_result(adeco_session *s, uint64_t batch_id, int index, double *host_out, size_t capacity)
+{
+    if (!s || !host_out) return fail(ADECO_ERR_ARGUMENT, "null argument");
+    auto b = find_batch(s, batch_id);
+    if (!b) return fail(ADECO_ERR_NOT_FOUND, "unknown batch %llu", (unsigned long long)batch_id);
+    if (index < 0 || index >= (int)b->reqs.size()) return fail(ADECO_ERR_ARGUMENT, "request index out of range");
+    int rc = adeco_session_wait(s, batch_id, 3600.0);
+    if (rc) return rc;
+    const size_t n = (size_t)b->reqs[index].dims * b->reqs[index].dims * b->reqs[index].dims;
+    if (capacity < n) return fail(ADECO_ERR_ARGUMENT, "capacity %zu < %zu cells", capacity, n);
+    std::vector<unsigned long long> tmp(n);
+    CUDA_TRY(cudaMemcpy(tmp.data(), b->d_fixed.p + b->offsets[index], n * sizeof(unsigned long long),
+                        cudaMemcpyDeviceToHost));
+    const double scale = std::ldexp(1.0, -b->grids[index].shift);
+    for (size_t c = 0; c < n; ++c) host_out[c] = (double)tmp[c] * scale;
+    return ADECO_OK;
+}
+
+extern "C" int adeco_session_latency(adeco_session *s, uint64_t batch_id, int index, double *ms)
+{
+    if (!s || !ms) return fail(ADECO_ERR_ARGUMENT, "null argument");
+    auto b = find_batch(s, batch_id);
+    if (!b) return fail(ADECO_ERR_NOT_FOUND, "unknown batch %llu", (unsigned long long)batch_id);
+    if (index < 0 || index >= (int)b->reqs.size()) return fail(ADECO_ERR_ARGUMENT, "request index out of range");
+    if (b->latency_ms < 0) return fail(ADECO_ERR_STATE, "batch not finished");
+    *ms = b->latency_ms;
+    return ADECO_OK;
+}
+
+extern "C" int adeco_session_release(adeco_session *s, uint64_t batch_id)
+{
+    if (!s) return fail(ADECO_ERR_ARGUMENT, "null session");
+    std::shared_ptr<adeco_session::Batch> b;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        auto it = s->batches.find(batch_id);
+        if (it == s->batches.end()) return fail(ADECO_ERR_NOT_FOUND, "unknown batch");
+        b = it->second;
+        s->batches.erase(it);
+    }
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    return ADECO_OK;
+}

@@ -1,0 +1,247 @@
+"""GPU parity: the CUDA path (through the C ABI) against the oracle and the
+reference-made golden fixtures.
+
+Bars:
+* tet connectivity and per-tet candidate ranges / per-cell candidate counts:
+  bit-exact;
+* octree topology: bit-exact;
+* cell masses: |gpu - fp64| <= REL * fp64 + ABS per cell, REL = 1e-5, with
+  ABS = 1e-9 tet masses (a floor far below any cell a tet overlaps by more
+  than a sliver);
+* total mass: within 1e-9 relative at workload scale (>= 10^6 tets, asserted
+  in test_total_mass_workload_scale).  The mixed path's per-tet mass error is
+  random with a standard deviation of about 1e-7 (FP32 clipping arithmetic),
+  so on the few-thousand-tet golden lattices the total is checked against
+  that statistical bound, 1e-9 * M + 3e-7 * sqrt(N_tets).
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, load_golden
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-5
+ABS = 1e-9
+
+
+@pytest.fixture(scope="module")
+def adeco():
+    from adeco_gb300 import build, deposit
+    build.build()
+    return deposit
+
+
+def check_cells(got, ref, rel=REL, abs_=ABS, n_tets=0):
+    got = np.asarray(got, np.float64).reshape(-1)
+    ref = np.asarray(ref, np.float64).reshape(-1)
+    bad = np.abs(got - ref) > rel * np.abs(ref) + abs_
+    assert not bad.any(), (f"{bad.sum()} cells out of tolerance; worst abs {np.abs(got - ref).max():.3e}; "
+                           f"e.g. got {got[bad][:3]} ref {ref[bad][:3]}")
+    if ref.sum() > 0:
+        assert abs(got.sum() - ref.sum()) <= 1e-9 * ref.sum() + 3e-7 * np.sqrt(n_tets) + 1e-12
+
+
+LATTICES = sorted(glob.glob(os.path.join(GOLDEN, "lattice_*.npz")))
+
+
+@pytest.mark.parametrize("path", LATTICES)
+def test_tet_connectivity_and_ranges_bitexact(adeco, oracle, path):
+    g = dict(np.load(path))
+    m, dims = int(g["m"]), int(g["dims"])
+    for order in (oracle.ORDER_REF, oracle.ORDER_CONFORMING):
+        rec, cand = adeco.tet_records(g["positions"], m, g["bbox"], dims, tet_order=order, counts=True)
+        ref = oracle.tet_records(g["positions"], m, g["bbox"], dims, order=order)
+        assert np.array_equal(rec, ref)
+        _, ocand = oracle.deposit_patches(g["positions"], m, g["bbox"], dims, fp64=False, order=order, counts=True)
+        assert np.array_equal(cand, ocand)
+
+
+@pytest.mark.parametrize("path", LATTICES)
+@pytest.mark.parametrize("precision", [0, 1], ids=["mixed", "plain_fp64"])
+def test_lattice_deposit_vs_reference_fp64(adeco, path, precision):
+    g = dict(np.load(path))
+    m, dims = int(g["m"]), int(g["dims"])
+    nt = 6 * m ** 3 if precision == 0 else 0
+    # plain FP64 clips in a different (cancellation-free) order than the
+    # reference's FP64 instantiation: both exact to rounding, ~1e-12 apart
+    tol = dict(rel=REL, abs_=ABS) if precision == 0 else dict(rel=1e-10, abs_=1e-12)
+    got = adeco.deposit_tets_ex(g["positions"], m, g["bbox"], dims, precision=precision)
+    check_cells(got, g["grid_f64"], n_tets=nt, **tol)
+    if g["conf_f64"].size:
+        got = adeco.deposit_tets_ex(g["positions"], m, g["bbox"], dims, precision=precision, tet_order=1)
+        check_cells(got, g["conf_f64"], n_tets=nt, **tol)
+
+
+def test_reference_boundary_accumulates_float(adeco):
+    """DepositWrapper.deposit_tets: float grid, +=, same meaning as the reference."""
+    g = load_golden("lattice_lat12_d3.npz")
+    m, dims = int(g["m"]), int(g["dims"])
+    data = np.zeros(dims ** 3, np.float32)
+    adeco.DepositWrapper.deposit_tets(True, 0, 0, 1, g["positions"], g["positions"].size, m, g["bbox"], dims, data)
+    check_cells(data, g["grid_f64"], rel=1e-6 + REL, abs_=1e-6, n_tets=6 * m ** 3)
+    first = data.copy()
+    adeco.DepositWrapper.deposit_tets(False, 0, 0, 1, g["positions"], g["positions"].size, m, g["bbox"], dims, data)
+    assert np.allclose(data, 2 * first, rtol=1e-6, atol=1e-6)
+    # against the reference's own FP32 result: its error vs FP64 is the bound
+    ref32 = g["grid_f32"].astype(np.float64)
+    err_ref = np.abs(ref32 - g["grid_f64"]).max()
+    assert np.abs(first - g["grid_f64"]).max() <= err_ref + 1e-6
+
+
+def test_padded_patch_sequence(adeco, oracle):
+    g = load_golden("patches_padded.npz")
+    m, dims = int(g["m"]), int(g["dims"])
+    kw = dict(patch_offset=int(g["patch_offset"]), num_patches=int(g["num_patches"]))
+    ref = oracle.deposit_patches(g["positions"], m, g["bbox"], dims, fp64=True, **kw)
+    got = adeco.deposit_tets_ex(g["positions"], m, g["bbox"], dims, **kw)
+    check_cells(got, ref, n_tets=6 * m ** 3 * int(g["num_patches"]))
+    assert np.abs(g["grid_f32"] - ref).max() < 1e-3  # the fixture is the reference's FP32 of the same call
+
+
+def test_random_lattice_vs_oracle(adeco, oracle):
+    from adeco_gb300.synthetic import zeldovich_lattice
+    for seed, n, disp, dims in ((11, 20, 1.0, 24), (12, 16, 4.0, 40), (13, 14, 0.3, 7)):
+        pos = zeldovich_lattice(n, L=30.0, seed=seed, rms_disp=disp)
+        p = pos.reshape(-1, 3)
+        lo, hi = float(p.min()) + 1.0, float(p.max()) - 2.0
+        bb = np.array([lo, hi, lo, hi, lo, hi], np.float32)
+        ref = oracle.deposit_patches(pos.reshape(-1), n - 1, bb, dims, fp64=True)
+        got = adeco.deposit_tets_ex(pos.reshape(-1), n - 1, bb, dims)
+        check_cells(got, ref, n_tets=6 * (n - 1) ** 3)
+
+
+def test_deterministic_bitwise(adeco):
+    g = load_golden("lattice_lat12_d3.npz")
+    m, dims = int(g["m"]), int(g["dims"])
+    a = adeco.deposit_tets_ex(g["positions"], m, g["bbox"], dims)
+    b = adeco.deposit_tets_ex(g["positions"], m, g["bbox"], dims)
+    assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
+
+
+def test_empty_input_is_a_no_op(adeco):
+    data = np.ones(8, np.float32)
+    adeco.DepositWrapper.deposit_tets(False, 0, 0, 0, np.zeros(0, np.float32), 0, 7,
+                                      np.array([0, 1, 0, 1, 0, 1], np.float32), 2, data)
+    assert np.all(data == 1)
+
+
+def test_errors_raise_like_the_reference(adeco):
+    g = load_golden("lattice_lat9_d0.5.npz")
+    m, dims = int(g["m"]), int(g["dims"])
+    data = np.zeros(dims ** 3, np.float32)
+    pos = g["positions"]
+    with pytest.raises(adeco.AdRuntimeException) as e:       # inconsistent offset
+        adeco.DepositWrapper.deposit_tets(False, 0, 1, 1, pos, pos.size, m, g["bbox"], dims, data)
+    assert e.value.code == 6
+    with pytest.raises(adeco.AdRuntimeException) as e:       # invalid device id
+        adeco.DepositWrapper.deposit_tets(True, 4096, 0, 1, pos, pos.size, m, g["bbox"], dims, data)
+    assert e.value.code == 3
+    with pytest.raises(adeco.AdRuntimeException) as e:       # positions not a whole number of patches
+        adeco.DepositWrapper.deposit_tets(False, 0, 0, 1, pos[:-3], pos.size - 3, m, g["bbox"], dims, data)
+    assert e.value.code == 1
+    with pytest.raises(adeco.AdRuntimeException) as e:       # int overflow of the cube counter
+        adeco.DepositWrapper.deposit_tets(False, 0, 0, 1 << 26, pos, pos.size, m, g["bbox"], dims, data)
+    assert e.value.code == 2
+    assert np.all(data == 0)
+
+
+def test_octree_topology_and_leaves(adeco, oracle):
+    g = load_golden("octree.npz")
+    n = int(g["n"])
+    pos = g["positions"].reshape(n, n, n, 3)
+    d = int(g["leaf_dims"])
+    with adeco.Session(pos) as s:
+        box = g["box"]
+        info = s.build_octree(int(g["max_tets"]), int(g["max_level"]), leaf_dims=d, box6=box, roi6=g["roi"])
+        nodes = info.nodes
+        assert len(nodes) == len(g["node_f"])
+        assert np.array_equal(np.stack([nodes["min"][:, 0], nodes["min"][:, 1], nodes["min"][:, 2], nodes["ext"]], 1),
+                              g["node_f"])
+        assert np.array_equal(nodes["level"], g["node_i"][:, 0])
+        assert np.array_equal(nodes["parent"], g["node_i"][:, 1])
+        assert np.array_equal(nodes["first_child"], g["node_i"][:, 2])
+        assert np.array_equal(nodes["estimate"], g["node_est"])
+        assert np.array_equal(info.leaves, g["leaf_ids"])
+        for q in range(len(info.leaves)):
+            ref_ids = g["leaf_meta_ids"][g["leaf_meta_off"][q]:g["leaf_meta_off"][q + 1]]
+            assert np.array_equal(s.leaf_meta(q), ref_ids)
+        grids, _ = s.deposit_leaves()
+        plain, _ = s.deposit_leaves(precision=1)
+        for q, nid in enumerate(info.leaves):
+            lb = adeco.leaf_bbox(nodes[nid])
+            ref = oracle.deposit_meta(g["positions"], (n, n, n), s.leaf_meta(q), lb, d, fp64=True)
+            check_cells(grids[q], ref, n_tets=2058 * len(s.leaf_meta(q)))
+            check_cells(plain[q], ref, rel=1e-10, abs_=1e-12)
+            if q < len(g["leaf_grids"]):  # the reference's own FP32 leaf deposit
+                assert np.abs(g["leaf_grids"][q] - ref).max() < 1e-3
+        # every tet lies in the root box and the leaves tile it; the leaves'
+        # FP32 boxes (min + ext per axis, as the reference forms them) meet to
+        # within an ulp, so the FP64 total is the tet count to ~1e-8
+        total = 6 * (n - 1) ** 3
+        assert abs(plain.sum() - total) <= 1e-7 * total
+        assert abs(grids.sum() - plain.sum()) <= 1e-9 * total + 3e-7 * np.sqrt(total)
+
+
+def test_total_mass_workload_scale(adeco):
+    """Total mass at workload scale: a 96^3 Zel'dovich lattice (5.1M tets).
+    Octree leaves: the mixed total equals the plain FP64 total of the same
+    leaves to 1e-9 (the leaves' FP32 boxes, formed as the reference forms
+    them, meet only to an ulp, so the FP64 total itself is the tet count to
+    ~1e-8).  Uniform 128^3 grid over a box holding every particle: the total
+    equals the tet count to 1e-9."""
+    from adeco_gb300.synthetic import zeldovich_lattice
+    n = 96
+    pos = zeldovich_lattice(n, L=100.0, seed=0, rms_disp=3.0)
+    total = 6 * (n - 1) ** 3
+    with adeco.Session(pos) as s:
+        s.build_octree(262144 // 8, 8, leaf_dims=16)
+        grids, t = s.deposit_leaves(stats=True)
+        plain, _ = s.deposit_leaves(precision=1)
+        # the mixed total against the FP64 total of the same leaves
+        assert abs(grids.sum() - plain.sum()) <= 1e-9 * total, grids.sum() - plain.sum()
+        assert abs(plain.sum() - total) <= 1e-7 * total
+        assert t["tets"] >= total
+    p = pos.reshape(-1, 3)
+    lo, hi = float(p.min()) - 0.5, float(p.max()) + 0.5
+    bb = np.array([lo, hi, lo, hi, lo, hi], np.float32)
+    got = adeco.deposit_tets_ex(pos.reshape(-1), n - 1, bb, 128)
+    assert abs(got.sum() - total) <= 1e-9 * total, got.sum() - total
+
+
+def test_graph_replay_matches_launch(adeco):
+    g = load_golden("octree.npz")
+    n = int(g["n"])
+    pos = g["positions"].reshape(n, n, n, 3)
+    with adeco.Session(pos) as s:
+        s.build_octree(int(g["max_tets"]), int(g["max_level"]), leaf_dims=8)
+        a, _ = s.deposit_leaves()
+        s.replay_leaves(3)
+        _, nvals = s.leaf_grids_device()
+        b, _ = s.deposit_leaves()
+        assert nvals == a.size
+        assert np.array_equal(a, b)
+
+
+def test_zoom_batch_same_alone_and_in_mix(adeco):
+    from adeco_gb300.synthetic import zeldovich_lattice
+    pos = zeldovich_lattice(24, L=40.0, seed=7, rms_disp=2.0)
+    reqs = [((20.0, 20.0, 20.0), 6.0, 16), ((10.0, 25.0, 18.0), 10.0, 24), ((30.0, 12.0, 22.0), 3.0, 32)]
+    with adeco.Session(pos) as s:
+        alone = []
+        for r in reqs:
+            b = s.submit([r])
+            s.wait(b)
+            alone.append(s.result(b, 0, r[2]))
+            s.release(b)
+        b1 = s.submit(reqs[:2])
+        b2 = s.submit(reqs[2:])
+        s.wait(b1)
+        s.wait(b2)
+        mixed = [s.result(b1, 0, reqs[0][2]), s.result(b1, 1, reqs[1][2]), s.result(b2, 0, reqs[2][2])]
+        for a, m_ in zip(alone, mixed):
+            assert np.array_equal(a, m_)
+        assert s.latency_ms(b1, 0) > 0
