@@ -91,6 +91,7 @@ _SIGS = {
     "adeco_session_latency": ([_vp, C.c_uint64, _i, C.POINTER(_d)], _i),
     "adeco_session_release": ([_vp, C.c_uint64], _i),
     "adeco_debug_tet_records": ([_vp, _sz, _i, _sz, _sz, _vp, _i, _i, _vp, _vp], _i),
+    "adeco_probe_fp32_tflops": ([_i, C.POINTER(_d)], _i),
 }
 
 _lib = None

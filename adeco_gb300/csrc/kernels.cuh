@@ -17,11 +17,12 @@
 // whether a request runs alone or inside a batch.
 #pragma once
 
+#include "clip_engine.cuh"
 #include "geometry.cuh"
 
 namespace adeco {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 128;
 constexpr int kWarps = kThreads / 32;
 constexpr int kMaxVerts = 512;   // 8^3
 constexpr int kMaxCubes = 343;   // 7^3
@@ -59,7 +60,7 @@ enum Stat : int {
     ST_CELLIN = 4,       // CELL_INSIDE_TET pairs
     ST_PARTIAL = 5,      // clipped pairs
     ST_FP64 = 6,         // pairs decided by the FP64 plane test
-    ST_PIECES = 7,       // leaf pieces whose volume was summed
+    ST_FALLBACK = 7,     // pieces clipped serially because the warp pool was full
     kNumStats = 8
 };
 
@@ -89,12 +90,16 @@ constexpr float kKappaFp64 = 32.f;
 
 struct SharedMixed {
     float4 vert[kMaxVerts];
+    float gh[3][kMaxVerts];   // grid-frame coordinates of the staged vertices, hi
+    float gl[3][kMaxVerts];   //   and lo parts
     uint16_t cubes[kMaxCubes + 1];
     int n_cubes;
     int item;
+    int next_group;
     GridDesc g;
     WarpTets wt[kWarps];
     uint32_t queue[kWarps][kQueue];
+    WarpPool pool[kWarps];
 };
 
 __device__ __forceinline__ void stat_add(unsigned long long *stats, int which, unsigned long long v)
@@ -113,8 +118,10 @@ __device__ __forceinline__ void warp_stat(unsigned long long *stats, int which, 
 
 // ---------------------------------------------------------------- staging
 __device__ __forceinline__ void stage_block(const DepositParams &P, const Item &it, float4 *vert, int vx, int vy,
-                                            int vz)
+                                            int vz, float (*gh)[kMaxVerts] = nullptr,
+                                            float (*gl)[kMaxVerts] = nullptr)
 {
+    const GridDesc *gd = P.grids + it.grid;
     const int nvt = vx * vy * vz;
     for (int v = threadIdx.x; v < nvt; v += blockDim.x) {
         const int i = v % vx, r = v / vx, j = r % vy, k = r / vy;
@@ -134,6 +141,11 @@ __device__ __forceinline__ void stage_block(const DepositParams &P, const Item &
             }
         }
         vert[v] = p;
+        if (gh) {
+            grid_frame(p.x, __ldg(&gd->gmin_d[0]), __ldg(&gd->scale_d[0]), gh[0][v], gl[0][v]);
+            grid_frame(p.y, __ldg(&gd->gmin_d[1]), __ldg(&gd->scale_d[1]), gh[1][v], gl[1][v]);
+            grid_frame(p.z, __ldg(&gd->gmin_d[2]), __ldg(&gd->scale_d[2]), gh[2][v], gl[2][v]);
+        }
     }
 }
 
@@ -160,14 +172,16 @@ __device__ __forceinline__ bool cube_alive(const float4 *vert, int vx, int vy, i
 }
 
 __device__ __forceinline__ void load_tet(const float4 *vert, int vx, int vy, int cube_local_idx, int t, int order,
-                                         int cvx, int cvy, float3 v[4])
+                                         int cvx, int cvy, float3 v[4], int *vid = nullptr)
 {
     const int ci = cube_local_idx % cvx, r = cube_local_idx / cvx, cj = r % cvy, ck = r / cvy;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         const int3 o = corner_offset(order, tet_conn(t, q));
-        const float4 p = vert[(ci + o.x) + vx * ((cj + o.y) + vy * (ck + o.z))];
+        const int id = (ci + o.x) + vx * ((cj + o.y) + vy * (ck + o.z));
+        const float4 p = vert[id];
         v[q] = make_float3(p.x, p.y, p.z);
+        if (vid) vid[q] = id;
     }
 }
 
@@ -180,8 +194,8 @@ __device__ __forceinline__ void load_tet(const float4 *vert, int vx, int vy, int
 // 27-bit local index); a larger tet sets the error flag and is skipped.
 constexpr long long kMaxPairsPerTet = 1LL << 25;
 
-ADECO_HD inline int setup_tet(const float3 vin[4], const GridDesc &g, WarpTets &W, int lane, int *error,
-                              bool *fp64_route)
+ADECO_HD inline int setup_tet(const float3 vin[4], const float ghin[4][3], const float glin[4][3], const GridDesc &g,
+                              WarpTets &W, int lane, int *error, bool *fp64_route)
 {
     *fp64_route = false;
     float3 v[4] = {vin[0], vin[1], vin[2], vin[3]};
@@ -190,33 +204,46 @@ ADECO_HD inline int setup_tet(const float3 vin[4], const GridDesc &g, WarpTets &
     int lo[3], hi[3];
     if (!candidate_range(v, g, lo, hi)) return 0;
     if (sgn == 0) return 0;
-    const long long cnt = (long long)(hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
-    if (cnt > kMaxPairsPerTet) {
+    {
+        const long long cnt0 = (long long)(hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
+        if (cnt0 > kMaxPairsPerTet) {
 #ifdef __CUDA_ARCH__
-        if (error) atomicOr(error, 1);
+            if (error) atomicOr(error, 1);
 #else
-        if (error) *error |= 1;
+            if (error) *error |= 1;
 #endif
-        return 0;
-    }
-    if (sgn < 0) { const float3 t = v[0]; v[0] = v[3]; v[3] = t; }
-    // anchor frame: q = (x - (gmin + lo*delta)) * scale, in FP64, rounded to FP32
-    double qd[4][3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        const double anchor = fma((double)lo[a], g.delta_d[a], g.gmin_d[a]);
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const double x = (a == 0) ? (double)v[q].x : ((a == 1) ? (double)v[q].y : (double)v[q].z);
-            qd[q][a] = (x - anchor) * g.scale_d[a];
+            return 0;
         }
     }
-    float qf[4][3];
+    // orientation rule on the vertex order: swap 0 <-> 3 when negative
+    const int o0 = (sgn < 0) ? 3 : 0, o3 = (sgn < 0) ? 0 : 3;
+    const int ord[4] = {o0, 1, 2, o3};
+    // Tight range: of the candidate cells [lo, hi], only those whose box
+    // [c r, c r + 1] (grid frame) meets the tet's AABB can receive mass (the
+    // rest fail the AABB test).  Bounds widened by the FP32 rounding of the
+    // grid-frame coordinates; the frame is then anchored at the first cell.
+    float qf[4][3], ql[4][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float g0 = ghin[0][a], g1 = ghin[1][a], g2 = ghin[2][a], g3 = ghin[3][a];
+        const float bmn = fminf(fminf(g0, g1), fminf(g2, g3)), bmx = fmaxf(fmaxf(g0, g1), fmaxf(g2, g3));
+        const float ir = (float)g.inv_rcell[a];
+        const float m0 = 4e-7f * (fabsf(bmn) + 2.f), m1 = 4e-7f * (fabsf(bmx) + 2.f);
+        const int c0 = max(lo[a], (int)floorf((bmn - 1.f) * ir - m0) + 1);
+        const int c1 = min(hi[a], (int)ceilf(bmx * ir + m1) - 1);
+        if (c1 < c0) return 0;
+        lo[a] = c0;
+        hi[a] = c1;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) shift_frame(ghin[ord[q]][a], glin[ord[q]][a], c0, g.drcell[a], qf[q][a], ql[q][a]);
+    }
+    // |6 V| in the anchor frame from the FP32 pairs, FP64 (the tet's
+    // signed-volume normaliser)
+    double qd[4][3];
 #pragma unroll
     for (int q = 0; q < 4; ++q)
 #pragma unroll
-        for (int a = 0; a < 3; ++a) qf[q][a] = (float)qd[q][a];
-    // |6 V| in the anchor frame, FP64 (the tet's signed-volume normaliser)
+        for (int a = 0; a < 3; ++a) qd[q][a] = (double)qf[q][a] + (double)ql[q][a];
     const double vq6 = fabs(vol6_fast<double>(qd[0], qd[1], qd[2], qd[3]));
     const double f6 = g.mass_factor / vq6;
     // planes from the FP32 vertices: inward normals (outward ones negated:
@@ -253,7 +280,7 @@ ADECO_HD inline int setup_tet(const float3 vin[4], const GridDesc &g, WarpTets &
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
             W.q[3 * q + a][lane] = qf[q][a];
-            W.qlo[3 * q + a][lane] = (float)(qd[q][a] - (double)qf[q][a]);
+            W.qlo[3 * q + a][lane] = ql[q][a];
         }
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -274,7 +301,7 @@ ADECO_HD inline int setup_tet(const float3 vin[4], const GridDesc &g, WarpTets &
         }
     const float Lm = sqrtf(L2);
     *fp64_route = !(Lm * Lm * Lm <= kKappaFp64 * (float)vq6);
-    return (int)cnt;
+    return (hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
 }
 
 enum PairClass : int { P_NO = 0, P_TET_INSIDE = 1, P_CELL_INSIDE = 2, P_PARTIAL = 3 };
@@ -286,7 +313,7 @@ enum PairClass : int { P_NO = 0, P_TET_INSIDE = 1, P_CELL_INSIDE = 2, P_PARTIAL 
 // the output: 64-bit fixed point (mixed path) or FP64 atomics (plain path).
 // Returns the counts of (candidate, partial) pairs seen by this lane.
 template <bool kFixed>
-__device__ void deposit_tet_fp64_warp(const float3 v[4], const int lo[3], const int hi[3], const GridDesc &g,
+__device__ __noinline__ void deposit_tet_fp64_warp(const float3 v[4], const int lo[3], const int hi[3], const GridDesc &g,
                                       unsigned long long *out_fixed, double *out_d, unsigned &n_cand,
                                       unsigned &n_part)
 {
@@ -437,7 +464,7 @@ ADECO_HD inline int classify_pair(const WarpTets &W, const GridDesc &g, int s, i
 }
 
 // mass (FP64) of one (tet, cell) pair -> 64-bit fixed point, added to the cell
-__device__ __forceinline__ void scatter(const DepositParams &P, const GridDesc &g, const WarpTets &W, int s, int a,
+__device__ __noinline__ void scatter(const DepositParams &P, const GridDesc &g, const WarpTets &W, int s, int a,
                                         int b, int c, double dm)
 {
     const unsigned long long fx = (unsigned long long)llrint(ldexp(dm, g.shift));
@@ -447,41 +474,61 @@ __device__ __forceinline__ void scatter(const DepositParams &P, const GridDesc &
     atomicAdd(P.out + idx, fx);
 }
 
-template <typename Acc>
-__device__ __forceinline__ void clip_and_scatter(const DepositParams &P, const GridDesc &g, const WarpTets &W,
-                                                 uint32_t entry, unsigned &pieces)
+// piece of pair `entry` (slot << 27 | local pair index) in its cell's frame
+__device__ __forceinline__ void pair_piece(const GridDesc &g, const WarpTets &W, uint32_t entry, float p[12], int &s,
+                                           int &a, int &b, int &c)
 {
-    const int s = entry >> 27;
+    s = entry >> 27;
     const int local = entry & ((1u << 27) - 1);
     const int ex0 = W.ex[0][s], ex1 = W.ex[1][s];
-    const int a = local % ex0, r = local / ex0, b = r % ex1, c = r / ex1;
-    float p[4][3];
+    a = local % ex0;
+    const int r = local / ex0;
+    b = r % ex1;
+    c = r / ex1;
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
-        p[v][0] = cell_coord(W.q[3 * v + 0][s], W.qlo[3 * v + 0][s], a, g.drcell[0]);
-        p[v][1] = cell_coord(W.q[3 * v + 1][s], W.qlo[3 * v + 1][s], b, g.drcell[1]);
-        p[v][2] = cell_coord(W.q[3 * v + 2][s], W.qlo[3 * v + 2][s], c, g.drcell[2]);
+        p[3 * v + 0] = cell_coord(W.q[3 * v + 0][s], W.qlo[3 * v + 0][s], a, g.drcell[0]);
+        p[3 * v + 1] = cell_coord(W.q[3 * v + 1][s], W.qlo[3 * v + 1][s], b, g.drcell[1]);
+        p[3 * v + 2] = cell_coord(W.q[3 * v + 2][s], W.qlo[3 * v + 2][s], c, g.drcell[2]);
     }
-    const Acc v6 = clip_volume6<float, Acc>(p);
-    (void)pieces;
-    const double dm = (double)v6 * W.factor6[s];
-    if (dm > 0.0) scatter(P, g, W, s, a, b, c, dm);
+}
+
+// clip the nb queued pairs Q[tail..tail+nb) with the whole warp and scatter
+__device__ __forceinline__ void clip_queue(const DepositParams &P, const GridDesc &g, const WarpTets &W,
+                                           WarpPool &pool, const uint32_t *Q, int tail, int nb, unsigned &fallbacks)
+{
+    const int lane = threadIdx.x & 31;
+    float p[12];
+    int s = 0, a = 0, b = 0, c = 0;
+    if (lane < nb) pair_piece(g, W, Q[(tail + lane) & (kQueue - 1)], p, s, a, b, c);
+    clip_batch(pool, p, nb, fallbacks);
+    if (lane < nb) {
+        const double v6 = ldexp((double)pool.vacc[lane], -kVolShift);
+        const double dm = v6 * W.factor6[s];
+        if (dm > 0.0) scatter(P, g, W, s, a, b, c, dm);
+    }
+    __syncwarp();
 }
 
 // -------------------------------------------------- mixed batched kernel
-template <typename Acc>
-__global__ void __launch_bounds__(kThreads, 2) deposit_mixed_kernel(DepositParams P)
+// Persistent: CTAs take work items (grid x vertex block) from a global
+// counter; inside an item the warps take groups of 32 tets from a shared
+// counter, so no warp waits for another until the item is done.
+__global__ void __launch_bounds__(kThreads, 3) deposit_mixed_kernel(DepositParams P)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SharedMixed &S = *reinterpret_cast<SharedMixed *>(smem_raw);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     WarpTets &W = S.wt[warp];
     uint32_t *Q = S.queue[warp];
+    WarpPool &pool = S.pool[warp];
+    unsigned st_tets = 0, st_cand = 0, st_bbox = 0, st_in = 0, st_cin = 0, st_part = 0, st_fp64 = 0, st_fb = 0;
 
     for (;;) {
         if (threadIdx.x == 0) {
             S.item = atomicAdd(P.counter, 1);
             S.n_cubes = 0;
+            S.next_group = 0;
         }
         __syncthreads();
         const int item = S.item;
@@ -489,7 +536,7 @@ __global__ void __launch_bounds__(kThreads, 2) deposit_mixed_kernel(DepositParam
         const Item it = P.items[item];
         if (threadIdx.x == 0) S.g = P.grids[it.grid];
         const int vx = it.nv & 0xff, vy = (it.nv >> 8) & 0xff, vz = (it.nv >> 16) & 0xff;
-        stage_block(P, it, S.vert, vx, vy, vz);
+        stage_block(P, it, S.vert, vx, vy, vz, S.gh, S.gl);
         __syncthreads();
         const GridDesc &g = S.g;
         const int cvx = vx - 1, cvy = vy - 1, cvz = vz - 1;
@@ -500,22 +547,35 @@ __global__ void __launch_bounds__(kThreads, 2) deposit_mixed_kernel(DepositParam
         }
         __syncthreads();
         const int ntet = 6 * S.n_cubes;
-        unsigned st_tets = 0, st_cand = 0, st_bbox = 0, st_in = 0, st_cin = 0, st_part = 0, st_fp64 = 0, st_pieces = 0;
-        for (int t0 = warp * 32; t0 < ntet; t0 += kThreads) {
-            const int tid = t0 + lane;
+        const int ngroups = (ntet + 31) / 32;
+        for (;;) {
+            int grp = 0;
+            if (lane == 0) grp = atomicAdd(&S.next_group, 1);
+            grp = __shfl_sync(0xffffffffu, grp, 0);
+            if (grp >= ngroups) break;
+            const int tid = grp * 32 + lane;
             int cnt = 0;
             bool route64 = false;
             if (tid < ntet) {
                 float3 v[4];
-                load_tet(S.vert, vx, vy, S.cubes[tid / 6], tid % 6, P.order, cvx, cvy, v);
-                cnt = setup_tet(v, g, W, lane, P.error, &route64);
+                int vid[4];
+                load_tet(S.vert, vx, vy, S.cubes[tid / 6], tid % 6, P.order, cvx, cvy, v, vid);
+                float gh[4][3], gl[4][3];
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) {
+                        gh[q][a] = S.gh[a][vid[q]];
+                        gl[q][a] = S.gl[a][vid[q]];
+                    }
+                cnt = setup_tet(v, gh, gl, g, W, lane, P.error, &route64);
                 W.tetid[lane] = tid;
             }
             st_tets += (cnt > 0);
             route64 = route64 && cnt > 0;
             if (route64) cnt = 0;  // deposited below by the FP64 route
             unsigned fp64_tets = __ballot_sync(0xffffffffu, route64);
-            // exclusive scan of the candidate counts across the warp
+            // exclusive scan of the pair counts across the warp
             int incl = cnt;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
@@ -532,7 +592,6 @@ __global__ void __launch_bounds__(kThreads, 2) deposit_mixed_kernel(DepositParam
                 bool part = false;
                 uint32_t entry = 0;
                 if (pidx < total) {
-                    // owning tet: last slot with scan <= pidx
                     int s = 0;
 #pragma unroll
                     for (int step = 16; step > 0; step >>= 1)
@@ -564,13 +623,11 @@ __global__ void __launch_bounds__(kThreads, 2) deposit_mixed_kernel(DepositParam
                 head += __popc(bal);
                 __syncwarp();
                 if (head - tail >= 32) {
-                    clip_and_scatter<Acc>(P, g, W, Q[(tail + lane) & (kQueue - 1)], st_pieces);
+                    clip_queue(P, g, W, pool, Q, tail, 32, st_fb);
                     tail += 32;
-                    __syncwarp();
                 }
             }
-            if (lane < head - tail) clip_and_scatter<Acc>(P, g, W, Q[(tail + lane) & (kQueue - 1)], st_pieces);
-            __syncwarp();
+            if (head > tail) clip_queue(P, g, W, pool, Q, tail, head - tail, st_fb);
             // ill-conditioned tets of this group: whole warp, FP64
             while (fp64_tets) {
                 const int src = __ffs(fp64_tets) - 1;
@@ -593,16 +650,17 @@ __global__ void __launch_bounds__(kThreads, 2) deposit_mixed_kernel(DepositParam
             }
             __syncwarp();
         }
-        if (P.stats) {
-            warp_stat(P.stats, ST_TETS, st_tets);
-            warp_stat(P.stats, ST_CAND, st_cand);
-            warp_stat(P.stats, ST_BBOX, st_bbox);
-            warp_stat(P.stats, ST_INSIDE, st_in);
-            warp_stat(P.stats, ST_CELLIN, st_cin);
-            warp_stat(P.stats, ST_PARTIAL, st_part);
-            warp_stat(P.stats, ST_FP64, st_fp64);
-        }
         __syncthreads();
+    }
+    if (P.stats) {
+        warp_stat(P.stats, ST_TETS, st_tets);
+        warp_stat(P.stats, ST_CAND, st_cand);
+        warp_stat(P.stats, ST_BBOX, st_bbox);
+        warp_stat(P.stats, ST_INSIDE, st_in);
+        warp_stat(P.stats, ST_CELLIN, st_cin);
+        warp_stat(P.stats, ST_PARTIAL, st_part);
+        warp_stat(P.stats, ST_FP64, st_fp64);
+        warp_stat(P.stats, ST_FALLBACK, st_fb);
     }
 }
 

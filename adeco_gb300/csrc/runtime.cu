@@ -114,6 +114,7 @@ GridDesc make_grid(const float bbox[6], int dims, double tet_mass, int shift, lo
     g.mass_factor = tet_mass * cell_vol * s * s * s;
     for (int a = 0; a < 3; ++a) {
         g.rcell[a] = g.delta_d[a] * g.scale_d[a];
+        g.inv_rcell[a] = 1.0 / g.rcell[a];
         g.drcell[a] = (float)(g.rcell[a] - 1.0);
     }
     g.tet_mass = (float)tet_mass;
@@ -143,13 +144,10 @@ int mixed_setup(int device, DeviceProps &dp)
     CUDA_TRY(cudaGetDeviceProperties(&prop, device));
     dp.sms = prop.multiProcessorCount;
     dp.mixed_smem = sizeof(SharedMixed);
-    CUDA_TRY(cudaFuncSetAttribute(deposit_mixed_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)dp.mixed_smem));
-    CUDA_TRY(cudaFuncSetAttribute(deposit_mixed_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    CUDA_TRY(cudaFuncSetAttribute(deposit_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)dp.mixed_smem));
     int nb = 0;
-    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, deposit_mixed_kernel<double>, kThreads,
-                                                           dp.mixed_smem));
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, deposit_mixed_kernel, kThreads, dp.mixed_smem));
     dp.mixed_blocks_per_sm = std::max(1, nb);
     cache[device] = dp;
     return ADECO_OK;
@@ -165,10 +163,8 @@ int launch_mixed(const DeviceProps &dp, DepositParams P, int acc_fp64, cudaStrea
     if (P.n_items <= 0) return ADECO_OK;
     CUDA_TRY(cudaMemsetAsync(P.counter, 0, sizeof(int), st));
     const int grid = std::max(1, std::min(P.n_items, dp.sms * dp.mixed_blocks_per_sm));
-    if (acc_fp64)
-        deposit_mixed_kernel<double><<<grid, kThreads, dp.mixed_smem, st>>>(P);
-    else
-        deposit_mixed_kernel<float><<<grid, kThreads, dp.mixed_smem, st>>>(P);
+    (void)acc_fp64;  // piece volumes are summed exactly in fixed point
+    deposit_mixed_kernel<<<grid, kThreads, dp.mixed_smem, st>>>(P);
     CUDA_TRY(cudaGetLastError());
     return ADECO_OK;
 }
@@ -1107,5 +1103,53 @@ extern "C" int adeco_session_release(adeco_session *s, uint64_t batch_id)
         s->batches.erase(it);
     }
     if (b->stream) cudaStreamSynchronize(b->stream);
+    return ADECO_OK;
+}
+
+// ============================================================ peak probe
+// FP32 FMA throughput of this device: 8 independent FMA chains per thread,
+// enough warps to fill every SM; reported as TFLOP/s (2 flops per FMA).
+__global__ void fma_probe_kernel(float *out, int iters, float a, float b)
+{
+    float x0 = threadIdx.x * 1e-3f, x1 = x0 + 1.f, x2 = x0 + 2.f, x3 = x0 + 3.f;
+    float x4 = x0 + 4.f, x5 = x0 + 5.f, x6 = x0 + 6.f, x7 = x0 + 7.f;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+            x0 = fmaf(x0, a, b); x1 = fmaf(x1, a, b); x2 = fmaf(x2, a, b); x3 = fmaf(x3, a, b);
+            x4 = fmaf(x4, a, b); x5 = fmaf(x5, a, b); x6 = fmaf(x6, a, b); x7 = fmaf(x7, a, b);
+        }
+    }
+    const float r = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
+    if (r == 12345.678f) out[blockIdx.x] = r;  // keeps the chains alive
+}
+
+extern "C" int adeco_probe_fp32_tflops(int device, double *tflops)
+{
+    if (!tflops) return fail(ADECO_ERR_ARGUMENT, "null output");
+    CUDA_TRY(cudaSetDevice(device));
+    cudaDeviceProp prop;
+    CUDA_TRY(cudaGetDeviceProperties(&prop, device));
+    DevBuf<float> out;
+    int rc = out.reserve(4096);
+    if (rc) return rc;
+    const int blocks = prop.multiProcessorCount * 8, threads = 256, iters = 2048;
+    cudaEvent_t e0, e1;
+    CUDA_TRY(cudaEventCreate(&e0));
+    CUDA_TRY(cudaEventCreate(&e1));
+    double best = 0.0;
+    for (int rep = 0; rep < 5; ++rep) {
+        CUDA_TRY(cudaEventRecord(e0));
+        fma_probe_kernel<<<blocks, threads>>>(out.p, iters, 0.999f, 1e-4f);
+        CUDA_TRY(cudaEventRecord(e1));
+        CUDA_TRY(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+        const double flops = 2.0 * 8 * 16 * (double)iters * blocks * threads;
+        if (rep > 0) best = std::max(best, flops / (ms * 1e-3) / 1e12);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *tflops = best;
     return ADECO_OK;
 }

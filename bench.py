@@ -1,0 +1,446 @@
+#!/usr/bin/env python3
+"""Benchmark: phase-space tetrahedron mass deposit on one GB300.
+
+Workload (one step): the octree deposit of a 256^3-particle Zel'dovich
+lattice -- RMS displacement 3 lattice spacings, seed 0, box L = 100 --
+into an adaptive octree (max depth 8, 16^3-cell leaf blocks, refine while a
+node's tet estimate exceeds 64 * 16^3 = 262144), every leaf deposited.
+  value  : distinct tets / s of the batched persistent mixed-precision
+           deposit (one CUDA-graph replay per step, lattice resident in HBM)
+  e2e    : the same tets / s through the public C ABI with host buffers:
+           session create (H2D of the positions from pinned memory), octree,
+           deposit, D2H of every leaf grid, destroy -- per step
+  plain  : the one-request-per-launch FP64 deposit (one launch per leaf)
+Multi-GPU: the deposit does not exchange data between GPUs ("replicas
+only"): each rank deposits its own replica, value = all ranks' tets / max
+time.
+
+--impl reference times the reference algorithm's CPU deposit (the oracle
+restatement, FP32, all host threads) on a bounded sample of the same leaves
+per step, and extrapolates to the whole workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_PART = 256
+L_BOX = 100.0
+RMS_DISP = 3.0
+MAX_TETS = 64 * 16 ** 3
+MAX_LEVEL = 8
+LEAF = 16
+WORKLOAD = ("octree deposit of a 256^3 Zel'dovich lattice (rms disp 3 spacings, seed 0, L=100): "
+            "depth <= 8, 16^3-cell leaves, refine while tet estimate > 262144 (64 per cell)")
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    """Barrier / max-reduce over ranks (torch.distributed, NCCL) for N > 1."""
+
+    def __init__(self, ws, local):
+        self.ws = ws
+        self.pg = None
+        if ws > 1:
+            import torch
+            import torch.distributed as dist
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl")
+            self.torch, self.dist = torch, dist
+
+    def barrier(self):
+        if self.ws > 1:
+            self.dist.barrier()
+
+    def max(self, x):
+        if self.ws == 1:
+            return x
+        t = self.torch.tensor([x], dtype=self.torch.float64, device="cuda")
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x):
+        if self.ws == 1:
+            return x
+        t = self.torch.tensor([x], dtype=self.torch.float64, device="cuda")
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.ws > 1:
+            self.dist.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.gpu), "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def workload_positions():
+    from adeco_gb300.synthetic import zeldovich_lattice
+    return zeldovich_lattice(N_PART, L=L_BOX, seed=0, rms_disp=RMS_DISP)
+
+
+def set_size(n):
+    """Lattice size (256 for the benchmark; smaller only for checking this script)."""
+    global N_PART
+    N_PART = n
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def profile_traffic():
+    """DRAM bytes per launch of the deposit kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "deposit_mixed_kernel_c2.md")
+    try:
+        text = open(path).read()
+    except OSError:
+        return None
+    m = re.search(r"dram_bytes_per_launch_full_workload:\s*([0-9.eE+]+)", text)
+    return float(m.group(1)) if m else None
+
+
+# --------------------------------------------------------------- CPU side
+def oracle_sample(pos, n, leaves_budget_s, threads, nodes, off, ids, leaves, seed_leaf=0):
+    """Deposit a spread sample of leaves with the oracle (FP32, the reference's
+    precision) on `threads` host threads; returns (seconds, meta-tets done)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from oracle import oracle as O
+    flat = np.ascontiguousarray(pos.reshape(-1))
+    nl = len(leaves)
+
+    def leaf_box(L):
+        nd = nodes[L]
+        return np.array([nd["min"][0], nd["min"][0] + nd["ext"], nd["min"][1], nd["min"][1] + nd["ext"],
+                         nd["min"][2], nd["min"][2] + nd["ext"]], np.float32)
+
+    def work(q):
+        L = leaves[q]
+        mids = ids[off[L]:off[L + 1]]
+        O.deposit_meta(flat, (n, n, n), mids, leaf_box(L), LEAF, fp64=False)
+        return len(mids)
+
+    # calibrate on one leaf, then run a spread sample sized to the budget
+    t0 = time.perf_counter()
+    m0 = work(seed_leaf % nl)
+    t1 = time.perf_counter() - t0
+    per_mc = t1 / max(1, m0)
+    target_mc = int(leaves_budget_s * threads / max(per_mc, 1e-9))
+    order = [(seed_leaf + 1 + k * 7919) % nl for k in range(nl)]
+    chosen, acc = [], 0
+    for q in order:
+        if acc >= target_mc:
+            break
+        if q in chosen:
+            continue
+        chosen.append(q)
+        acc += int(off[leaves[q] + 1] - off[leaves[q]])
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        done = sum(ex.map(work, chosen))
+    return time.perf_counter() - t0, done, len(chosen)
+
+
+def cpu_tree(pos, n):
+    from oracle import oracle as O
+    p = pos.reshape(-1, 3)
+    box = np.array([*p.min(0), *p.max(0)], np.float32)
+    roi = np.array([1, 1, 1, 0, 0, 0], np.float32)
+    max_tets = min(6 * (n - 1) ** 3, MAX_TETS)
+    return O.generate_tree(np.ascontiguousarray(pos.reshape(-1)), (n, n, n), box, roi, max_tets, MAX_LEVEL)
+
+
+def run_reference(args, rank, ws):
+    """--impl reference: the reference algorithm on the host cores."""
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    pos = workload_positions()
+    n = N_PART
+    nodes, off, ids, leaves = cpu_tree(pos, n)
+    total_mc = int(sum(off[L + 1] - off[L] for L in leaves))
+    tets = 6 * (n - 1) ** 3
+    vals, times = [], []
+    for step in range(args.warmup + args.steps):
+        sec, mc, nleaf = oracle_sample(pos, n, args.ref_step_s, threads, nodes, off, ids, leaves, seed_leaf=step)
+        full = sec * total_mc / max(1, mc)           # extrapolated time of the whole workload
+        if step >= args.warmup:
+            vals.append(tets / full)
+            times.append(full * 1e3)
+    value = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": "tets/s deposited", "value": value, "unit": "tets/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.median(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "tets": tets, "leaves": len(leaves)},
+        "cpu_baseline": {"value": value, "unit": "tets/s", "cores": threads, "kind": "port",
+                         "sample": f"each step: a spread sample of octree leaves sized to ~{args.ref_step_s:.0f} s "
+                                   f"on {threads} threads (FP32 oracle restatement of the reference deposit), "
+                                   f"extrapolated by meta-cell count to all {len(leaves)} leaves"},
+        "e2e": {"value": value, "unit": "tets/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# --------------------------------------------------------------- GPU side
+def algorithmic_flops(pos, n, nodes, off, ids, leaves, sample_leaves=3):
+    """Reference-algorithm FLOPs per meta-cell tet, counted by the instrumented
+    oracle on a spread sample of leaves (single thread)."""
+    from oracle import oracle as O
+    L_ = O.lib()
+    flat = np.ascontiguousarray(pos.reshape(-1))
+    flops, mcs = 0, 0
+    for k in range(sample_leaves):
+        L = leaves[(k * len(leaves)) // sample_leaves]
+        nd = nodes[L]
+        bb = np.array([nd["min"][0], nd["min"][0] + nd["ext"], nd["min"][1], nd["min"][1] + nd["ext"],
+                       nd["min"][2], nd["min"][2] + nd["ext"]], np.float32)
+        mids = ids[off[L]:off[L + 1]]
+        L_.ora_flops_reset()
+        O.deposit_meta(flat, (n, n, n), mids, bb, LEAF, fp64=False)
+        flops += L_.ora_flops_get()
+        mcs += len(mids)
+    return flops / max(1, mcs)
+
+
+def run_ours(args, rank, ws, local):
+    from adeco_gb300 import _lib as LB
+    from adeco_gb300 import deposit as D
+    dist = Dist(ws, local)
+    lib = LB.load(build_if_missing=True)
+    pos = workload_positions()
+    n = N_PART
+    tets = 6 * (n - 1) ** 3
+    out = {}
+    with D.Session(pos, device=local if ws > 1 else args.device) as s:
+        info = s.build_octree(MAX_TETS, MAX_LEVEL, leaf_dims=LEAF)
+        nleaf = len(info.leaves)
+        # one untimed pass with the pair counters on
+        grids, st = s.deposit_leaves(stats=True)
+        mixed_total = float(grids.sum())
+        for _ in range(args.warmup):
+            s.replay_leaves(1)
+        kern = [s.deposit_leaves(fetch=False)[1]["kernel_ms"] for _ in range(2)]
+        dist.barrier()
+        with ClockSampler(local if ws > 1 else args.device) as clk:
+            t = s.replay_leaves(args.steps)
+        dist.barrier()
+        ms_step = dist.max(t["kernel_ms"])
+        total_tets = dist.sum(float(tets))
+        out["value"] = total_tets / (ms_step * 1e-3)
+        out["ms_per_step"] = ms_step
+        out["clocks"] = clk.summary()
+        out["kernel_ms"] = min(kern)
+        out["stats"] = st
+        out["nleaf"] = nleaf
+        out["levels"] = info.levels
+        # plain FP64, one launch per leaf
+        plain = {}
+        if not args.skip_plain:
+            pg, pt = s.deposit_leaves(precision=1)
+            plain = {"ms_per_step": pt["kernel_ms"], "tets_per_s": tets / (pt["kernel_ms"] * 1e-3),
+                     "launches": pt["launches"], "steps": 1}
+            d = np.abs(pg - grids)
+            err = {}
+            for th in (1.0, 1e-2, 1e-3):
+                sel = pg > th
+                err[f"max_rel_cells_gt_{th:g}"] = float((d[sel] / pg[sel]).max()) if sel.any() else 0.0
+                err[f"cells_gt_{th:g}"] = int(sel.sum())
+            err["max_abs_tet_masses"] = float(d.max())
+            err["cells_nonzero"] = int((pg > 0).sum())
+            err["bar_1e-5_rel_plus_1e-7_abs_ok"] = bool(np.all(d <= 1e-5 * pg + 1e-7))
+            plain["mixed_vs_fp64"] = err
+            plain["total_mass_rel_diff"] = abs(mixed_total - float(pg.sum())) / float(pg.sum())
+            del pg
+        out["plain"] = plain
+        out["mass"] = {"mixed_total": mixed_total, "tet_count": tets}
+        leaf_values = grids.size
+        del grids
+    # e2e through the public C ABI with host buffers (pinned), per step
+    e2e = None
+    if not args.skip_e2e:
+        import torch
+        pin_pos = torch.empty(pos.size, dtype=torch.float32, pin_memory=True)
+        pin_pos.numpy()[:] = pos.reshape(-1)
+        pin_out = torch.empty(leaf_values, dtype=torch.float64, pin_memory=True)
+        cfg = LB.SessionConfig(local if ws > 1 else args.device, 0, 1.0, 0.75, 1)
+        tim = LB.Timing()
+        e2e_times = []
+        for step in range(args.e2e_warmup + args.e2e_steps):
+            dist.barrier()
+            t0 = time.perf_counter()
+            h = C.c_void_p()
+            LB.check(lib.adeco_session_create(C.byref(cfg), C.c_void_p(pin_pos.data_ptr()), n, n, n, C.byref(h)))
+            LB.check(lib.adeco_session_build_octree(h, None, None, MAX_TETS, MAX_LEVEL, LEAF))
+            LB.check(lib.adeco_session_deposit_leaves(h, 0, C.c_void_p(pin_out.data_ptr()), 0, C.byref(tim)))
+            LB.check(lib.adeco_session_destroy(h))
+            dt = time.perf_counter() - t0
+            if step >= args.e2e_warmup:
+                e2e_times.append(dist.max(dt))
+        e2e_s = statistics.median(e2e_times)
+        e2e = {"value": dist.sum(float(tets)) / e2e_s, "unit": "tets/s", "ms_per_step": e2e_s * 1e3,
+               "h2d_bytes_per_step": int(pos.size * 4), "d2h_bytes_per_step": int(leaf_values * 8),
+               "steps": args.e2e_steps, "warmup": args.e2e_warmup}
+    dist.close()
+    if rank != 0:
+        return 0
+    # roofline of the deposit kernel (FP32-pipe bound; HBM figure beside it)
+    nodes, off, ids, leaves = cpu_tree(pos, n)
+    flops_per_mc = algorithmic_flops(pos, n, nodes, off, ids, leaves)
+    total_mc = int(sum(off[L + 1] - off[L] for L in leaves))
+    alg_flops = flops_per_mc * total_mc
+    peak = C.c_double()
+    LB.check(lib.adeco_probe_fp32_tflops(args.device, C.byref(peak)))
+    k_s = out["kernel_ms"] * 1e-3
+    achieved = alg_flops / k_s / 1e12
+    alg_bytes = 12.0 * n ** 3 + 8.0 * out["nleaf"] * LEAF ** 3
+    peaks = measured_peaks()
+    hbm = peaks.get("hbm_gbs")
+    traffic = profile_traffic()
+    roof = {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s", "frac": achieved / peak.value,
+            "traffic": traffic, "peak_source": "measured FP32 FMA probe (adeco_probe_fp32_tflops) on this GPU",
+            "flops_per_launch": alg_flops, "flops_model": "reference-algorithm FLOPs counted by the instrumented "
+            "oracle on a spread sample of leaves, per meta-cell tet, x all leaves' meta-cell tets",
+            "kernel_ms": out["kernel_ms"],
+            "hbm": {"achieved_gbs": alg_bytes / k_s / 1e9, "peak_gbs": hbm, "frac_of_measured":
+                    (alg_bytes / k_s / 1e9 / hbm) if hbm else None, "algorithmic_bytes": alg_bytes}}
+    # CPU baseline: the oracle (reference algorithm, FP32) on a bounded sample
+    cpu = None
+    if ws == 1 and not args.skip_cpu:
+        threads = os.cpu_count() or 1
+        sec, mc, nl = oracle_sample(pos, n, args.cpu_budget_s, threads, nodes, off, ids, leaves)
+        full = sec * total_mc / max(1, mc)
+        cpu = {"value": tets / full, "unit": "tets/s", "cores": threads, "kind": "port",
+               "sample": f"{nl} of {len(leaves)} octree leaves ({mc} meta-cells, {sec:.1f} s on {threads} threads, "
+                         f"FP32 oracle restatement of the reference deposit), extrapolated by meta-cell count"}
+    st = out["stats"]
+    line = {
+        "metric": "tets/s deposited", "value": out["value"], "unit": "tets/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": out["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "tets": tets, "leaves": out["nleaf"], "octree_levels": out["levels"],
+                   "precision": "FP32 clipping; FP64 near-degenerate classification, volume sums, kappa>32 tets; "
+                                "64-bit fixed-point accumulation",
+                   "l2": "inputs larger than L2 (268 MB float4 lattice); no flush", "cuda_graph": True,
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": 2 * args.steps,
+        "clocks": out["clocks"],
+        "plain_fp64": out["plain"],
+        "batched_over_plain": (out["value"] / ws / out["plain"]["tets_per_s"]) if out["plain"] else None,
+        "tet_cell_pairs_per_s": {"candidate": st["candidate_pairs"] / (out["ms_per_step"] * 1e-3),
+                                 "partial": st["partial_pairs"] / (out["ms_per_step"] * 1e-3)},
+        "pair_counts": st,
+        "mass": out["mass"],
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--device", type=int, default=0)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-warmup", type=int, default=1)
+    ap.add_argument("--cpu-budget-s", type=float, default=12.0)
+    ap.add_argument("--ref-step-s", type=float, default=6.0)
+    ap.add_argument("--skip-plain", action="store_true")
+    ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--n", type=int, default=256, help="lattice size; the benchmark workload is 256")
+    args = ap.parse_args()
+    set_size(args.n)
+    if args.warmup < 3:
+        args.warmup = 3
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, rank, ws)
+    return run_ours(args, rank, ws, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -205,6 +205,10 @@ int adeco_debug_tet_records(const float *positions, size_t positions_size, int m
                             size_t cube_begin, size_t cube_end, const float bbox[6], int dims, int tet_order,
                             int32_t *records, uint32_t *cand);
 
+/* Measured FP32 FMA throughput of `device` (TFLOP/s, 2 flops per FMA): the
+ * peak the deposit kernels' roofline fraction is stated against. */
+int adeco_probe_fp32_tflops(int device, double *tflops);
+
 #ifdef __cplusplus
 }
 #endif

@@ -6,8 +6,10 @@ Bars:
   bit-exact;
 * octree topology: bit-exact;
 * cell masses: |gpu - fp64| <= REL * fp64 + ABS per cell, REL = 1e-5, with
-  ABS = 1e-9 tet masses (a floor far below any cell a tet overlaps by more
-  than a sliver);
+  ABS = 1e-7 tet masses: FP32 clipping leaves an absolute error of a few
+  1e-8 tet masses in the cells a tet only grazes, so the bar is relative for
+  every cell holding more than 1e-2 of a tet's mass (all interior cells) and
+  absolute for the near-empty cells at the edge of the particle distribution;
 * total mass: within 1e-9 relative at workload scale (>= 10^6 tets, asserted
   in test_total_mass_workload_scale).  The mixed path's per-tet mass error is
   random with a standard deviation of about 1e-7 (FP32 clipping arithmetic),
@@ -25,7 +27,7 @@ from conftest import GOLDEN, load_golden
 pytestmark = pytest.mark.gpu
 
 REL = 1e-5
-ABS = 1e-9
+ABS = 1e-7
 
 
 @pytest.fixture(scope="module")
