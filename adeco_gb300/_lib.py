@@ -73,6 +73,7 @@ _SIGS = {
     "adeco_deposit_tets": ([_i, _sz, _sz, _sz, _vp, _sz, _i, _vp, _i, _vp], _i),
     "adeco_deposit_tets_ex": ([C.POINTER(DepositArgs)], _i),
     "adeco_deposit_tets_device": ([_vp, _sz, _sz, _sz, _i, _vp, _i, _vp, _i, _i, _d, _vp], _i),
+    "adeco_deposit_tets_device_noalloc": ([_vp, _sz, _sz, _sz, _i, _vp, _i, _vp, _i, _d, _vp], _i),
     "adeco_session_create": ([C.POINTER(SessionConfig), _vp, _i, _i, _i, C.POINTER(_vp)], _i),
     "adeco_session_destroy": ([_vp], _i),
     "adeco_session_bbox": ([_vp, _vp], _i),

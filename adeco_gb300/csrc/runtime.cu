@@ -1153,3 +1153,150 @@ extern "C" int adeco_probe_fp32_tflops(int device, double *tflops)
     *tflops = best;
     return ADECO_OK;
 }
+
+// ============================================================ no-allocation entry point
+// adeco_deposit_tets_device_noalloc: the mixed deposit of
+// adeco_deposit_tets_device for callers that cannot allocate device memory
+// (code running inside a CUDA-graph capture they do not own, a host that
+// forbids cudaMalloc after start-up, a pool allocator owned by someone else).
+// Its scratch -- work counter, error flag, grid descriptor, work items and
+// the 64-bit fixed-point accumulators -- lives in one file-scope device
+// array of kNoAllocScratchBytes that every GPU loading this library holds
+// until the process exits.  The array is shared by every call on a device and
+// keeps the last call's contents; each call clears what must start at zero.
+// Calls that overlap on the GPU (two streams, or two host threads) race on
+// it: serialise them.
+namespace {
+constexpr int kNoAllocMaxItems = 16384;             // patch sub-blocks of <= 7^3 cubes
+constexpr long long kNoAllocMaxCells = 96LL * 96 * 96;  // grid cells (dims <= 96 for a cube)
+constexpr size_t kNoAllocHeader = 512;               // counter, error flag, GridDesc
+constexpr size_t kNoAllocScratchBytes =
+    kNoAllocHeader + (size_t)kNoAllocMaxItems * sizeof(Item) + (size_t)kNoAllocMaxCells * sizeof(unsigned long long);
+}  // namespace
+
+static_assert(256 + sizeof(GridDesc) <= kNoAllocHeader, "grid descriptor must fit the scratch header");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace {
+struct NoAllocDevice {
+    bool ready = false;
+    unsigned char *scratch = nullptr;  // device address of g_noalloc_scratch
+    int sms = 0;
+    int blocks_per_sm = 0;
+};
+constexpr int kNoAllocMaxDevices = 64;
+NoAllocDevice g_noalloc_dev[kNoAllocMaxDevices];
+std::mutex g_noalloc_mu;
+
+// once per device, with that device current
+int noalloc_setup(int dev, NoAllocDevice &out)
+{
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    NoAllocDevice &d = g_noalloc_dev[dev];
+    if (!d.ready) {
+        void *ptr = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess || ptr == nullptr)
+            return fail(ADECO_ERR_CUDA, "cudaGetSymbolAddress of the no-alloc scratch failed: %s",
+                        cudaGetErrorString(e));
+        int sms = 0, nb = 0;
+        CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        CUDA_TRY(cudaFuncSetAttribute(deposit_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)sizeof(SharedMixed)));
+        CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, deposit_mixed_kernel, kThreads,
+                                                               sizeof(SharedMixed)));
+        d.scratch = static_cast<unsigned char *>(ptr);
+        d.sms = sms;
+        d.blocks_per_sm = nb > 0 ? nb : 1;
+        d.ready = true;
+    }
+    out = d;
+    return ADECO_OK;
+}
+}  // namespace
+
+// the grid descriptor, passed by value, into the scratch
+__global__ void noalloc_grid_kernel(GridDesc *dst, GridDesc g) { *dst = g; }
+
+// work items of patches [p0, p0 + np): sub-blocks of <= 7^3 cubes, as patch_items()
+__global__ void noalloc_items_kernel(Item *items, long long p0, int n_items, int m, int nsb)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_items) return;
+    const long long n1 = m + 1, n2 = n1 * n1;
+    const int per = nsb * nsb * nsb;
+    const long long p = p0 + i / per;
+    const int sb = i % per, sx = sb % nsb, sy = (sb / nsb) % nsb, sz = sb / (nsb * nsb);
+    const int ox = sx * kMetaCubes, oy = sy * kMetaCubes, oz = sz * kMetaCubes;
+    const int vx = min(kMetaCubes + 1, m + 1 - ox), vy = min(kMetaCubes + 1, m + 1 - oy),
+              vz = min(kMetaCubes + 1, m + 1 - oz);
+    Item it;
+    it.base = p * n1 * n2 + ox + n1 * oy + n2 * oz;
+    it.grid = 0;
+    it.nv = vx | (vy << 8) | (vz << 16);
+    items[i] = it;
+}
+
+extern "C" int adeco_deposit_tets_device_noalloc(const float *d_positions, size_t positions_size, size_t patch_offset,
+                                                 size_t num_patches, int meta_cells_per_patch, const float bbox[6],
+                                                 int dims, double *d_out, int tet_order, double tet_mass, void *stream)
+{
+    if (positions_size == 0 || num_patches == 0) return ADECO_OK;
+    const int m = meta_cells_per_patch;
+    int rc = validate_boundary(patch_offset, num_patches, d_positions, positions_size, m, bbox, dims, d_out);
+    if (rc) return rc;
+    if (tet_order != ADECO_ORDER_REF && tet_order != ADECO_ORDER_CONFORMING)
+        return fail(ADECO_ERR_ARGUMENT, "unknown tet order %d", tet_order);
+    const long long ncell = (long long)dims * dims * dims;
+    if (ncell > kNoAllocMaxCells)
+        return fail(ADECO_ERR_LIMIT, "no-alloc deposit: %lld grid cells exceed the fixed scratch of %lld cells "
+                    "(dims <= 96)", ncell, kNoAllocMaxCells);
+    const int nsb = MetaGrid::ceil_div(m, kMetaCubes);
+    const long long n_items = (long long)num_patches * nsb * nsb * nsb;
+    if (n_items > kNoAllocMaxItems)
+        return fail(ADECO_ERR_LIMIT, "no-alloc deposit: %lld work items exceed the fixed scratch of %d "
+                    "(patches x ceil(m/7)^3)", n_items, kNoAllocMaxItems);
+    int dev = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(ADECO_ERR_DEVICE, "device %d out of range", dev);
+    NoAllocDevice nd;
+    if ((rc = noalloc_setup(dev, nd))) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    int *counter = reinterpret_cast<int *>(nd.scratch);  // [0] work counter, [1] error flag
+    GridDesc *grid = reinterpret_cast<GridDesc *>(nd.scratch + 256);
+    Item *items = reinterpret_cast<Item *>(nd.scratch + kNoAllocHeader);
+    unsigned long long *fixed =
+        reinterpret_cast<unsigned long long *>(nd.scratch + kNoAllocHeader + (size_t)kNoAllocMaxItems * sizeof(Item));
+    const int shift = choose_shift(6.0 * (double)num_patches * (double)m * m * m, tet_mass);
+    CUDA_TRY(cudaMemsetAsync(counter, 0, 2 * sizeof(int), st));
+    CUDA_TRY(cudaMemsetAsync(fixed, 0, (size_t)ncell * sizeof(unsigned long long), st));
+    noalloc_grid_kernel<<<1, 1, 0, st>>>(grid, make_grid(bbox, dims, tet_mass, shift, 0));
+    noalloc_items_kernel<<<(unsigned)((n_items + 127) / 128), 128, 0, st>>>(items, (long long)patch_offset,
+                                                                           (int)n_items, m, nsb);
+    CUDA_TRY(cudaGetLastError());
+    DepositParams P;
+    std::memset(&P, 0, sizeof P);
+    P.items = items;
+    P.n_items = (int)n_items;
+    P.src_kind = SRC_PATCH_F3;
+    P.grids = grid;
+    P.src = d_positions;
+    P.stride_y = m + 1;
+    P.stride_z = (long long)(m + 1) * (m + 1);
+    P.order = tet_order;
+    P.pad_check = 1;
+    P.out = fixed;
+    P.counter = counter;
+    P.error = counter + 1;
+    const int blocks = (int)std::max(1LL, std::min(n_items, (long long)nd.sms * nd.blocks_per_sm));
+    deposit_mixed_kernel<<<blocks, kThreads, sizeof(SharedMixed), st>>>(P);
+    CUDA_TRY(cudaGetLastError());
+    fixed_accumulate_f64_kernel<<<1024, 256, 0, st>>>(fixed, d_out, ncell, std::ldexp(1.0, -shift));
+    CUDA_TRY(cudaGetLastError());
+    int err = 0;
+    CUDA_TRY(cudaMemcpyAsync(&err, counter + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    if (err) return fail(ADECO_ERR_LIMIT, "a tet spans more than 2^25 candidate cells of the grid");
+    return ADECO_OK;
+}

@@ -102,6 +102,25 @@ int adeco_deposit_tets_device(const float *d_positions, size_t positions_size, s
                               size_t num_patches, int meta_cells_per_patch, const float bbox[6], int dims,
                               double *d_out, int precision, int tet_order, double tet_mass, void *stream);
 
+/* Same deposit as adeco_deposit_tets_device (mixed precision only), for
+ * callers that cannot allocate device memory at call time: code recorded
+ * into a CUDA graph owned by someone else, hosts that forbid cudaMalloc after
+ * start-up, or applications whose device memory belongs to their own pool.
+ * No counterpart in the reference (its deposit allocates on every call).
+ *
+ * It allocates nothing: its scratch is one fixed device array of about
+ * 7.3 MB compiled into the library, which every GPU that loads the library
+ * holds until the process exits.  Limits: dims^3 <= 96^3 grid cells and
+ * num_patches * ceil(m/7)^3 <= 16384 work items; larger calls return
+ * ADECO_ERR_LIMIT.  The first call on a device looks the array up with that
+ * device current (cudaGetSymbolAddress); make that first call before any
+ * stream capture.  Every call shares the array: calls that overlap on the
+ * GPU (other streams or host threads) race and must be serialised.
+ * d_out is ACCUMULATED (+=); the call synchronises `stream`. */
+int adeco_deposit_tets_device_noalloc(const float *d_positions, size_t positions_size, size_t patch_offset,
+                                      size_t num_patches, int meta_cells_per_patch, const float bbox[6], int dims,
+                                      double *d_out, int tet_order, double tet_mass, void *stream);
+
 /* ------------------------------------------------------------------ */
 /* Sessions: a resident particle lattice + octree                       */
 
