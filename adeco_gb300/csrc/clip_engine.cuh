@@ -6,6 +6,8 @@
 //   * drops its piece (entirely outside a cell face it has not yet passed),
 //   * finishes it (inside all six faces): its 6x volume is added, as exact
 //     64-bit fixed point, to the accumulator of the pair it came from, or
+//   * at the last cell face it crosses, adds the inside fraction of its
+//     volume (from the edge parameters alone, no cut points), or
 //   * splits it by the next cell face it crosses into 1 or 3 inside pieces,
 //     keeps one and pushes the others onto a per-warp shared-memory pool;
 // then idle lanes pop pieces from the pool (last in, first out).  All lanes
@@ -87,6 +89,17 @@ ADECO_HD inline void cut_point(const float *pin, const float *pout, int axis, fl
 //   k = 3: (A, B, C, Xcd)  (A, B, Xcd, Xbd) (A, Xbd, Xcd, Xad)
 // written as one code path: four cut points E0..E3 chosen by k, then the
 // children's vertices picked by k.
+ADECO_HD inline void put(float *dst, const float *a, const float *b, const float *c, const float *d)
+{
+#pragma unroll
+    for (int x = 0; x < 3; ++x) {
+        dst[x] = a[x];
+        dst[3 + x] = b[x];
+        dst[6 + x] = c[x];
+        dst[9 + x] = d[x];
+    }
+}
+
 ADECO_HD inline int split_piece(const float p[12], int mask, int f, float c0[12], float c1[12], float c2[12])
 {
     const int axis = f >> 1;
@@ -139,6 +152,49 @@ ADECO_HD inline int split_piece(const float p[12], int mask, int f, float c0[12]
     return k1 ? 1 : 3;
 }
 
+// Fraction of piece p inside face f (mask = 4-bit inside flags, 0 < mask <
+// 15), from the edge parameters alone.  On an edge from inside vertex i to
+// outside vertex o the plane sits at t = (plane - x_i) / (x_o - x_i); with u =
+// 1 - t taken as (x_o - plane) / (x_o - x_i) so both keep their relative
+// precision, and with the vertices ordered A B C D (inside first):
+//   k = 1: t_AB t_AC t_AD                          (the corner tet at A)
+//   k = 2: t_BC t_BD + t_AC t_BD u_BC + t_AC t_AD u_BD   (the 3-tet prism)
+//   k = 3: 1 - u_AD u_BD u_CD = t_AD + u_AD (t_BD + u_BD t_CD)
+// Every term is non-negative, so the fraction carries a few ulps of relative
+// error and the inside volume needs no cut points and no child volumes.
+ADECO_HD inline float inside_fraction(const float p[12], int mask, int f)
+{
+    const int axis = f >> 1;
+    const float plane = (f & 1) ? 1.f : 0.f;
+    const int pm = split_perm(mask), k = split_kin(mask);
+    const float x0 = sel3(axis, p[0], p[1], p[2]), x1 = sel3(axis, p[3], p[4], p[5]);
+    const float x2 = sel3(axis, p[6], p[7], p[8]), x3 = sel3(axis, p[9], p[10], p[11]);
+    const float a = sel4(pm & 3, x0, x1, x2, x3), b = sel4((pm >> 2) & 3, x0, x1, x2, x3);
+    const float c = sel4((pm >> 4) & 3, x0, x1, x2, x3), d = sel4((pm >> 6) & 3, x0, x1, x2, x3);
+    // edges as in split_piece: k=1: AB AC AD; k=2: AC AD BC BD; k=3: AD BD CD
+    const float i0 = a, o0 = (k == 1) ? b : ((k == 2) ? c : d);
+    const float i1 = (k == 3) ? b : a, o1 = (k == 1) ? c : d;
+    const float i2 = (k == 1) ? a : ((k == 2) ? b : c), o2 = (k == 2) ? c : d;
+    const float i3 = b, o3 = d;
+    float t[4], u[4];
+    const float in[4] = {i0, i1, i2, i3}, out[4] = {o0, o1, o2, o3};
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        // round-to-nearest reciprocal: an approximate one biases the
+        // fractions of all pairs the same way and shows in the total mass
+#ifdef __CUDA_ARCH__
+        const float r = __frcp_rn(out[e] - in[e]);
+#else
+        const float r = 1.f / (out[e] - in[e]);
+#endif
+        t[e] = fminf(fmaxf((plane - in[e]) * r, 0.f), 1.f);
+        u[e] = fminf(fmaxf((out[e] - plane) * r, 0.f), 1.f);
+    }
+    if (k == 1) return t[0] * t[1] * t[2];
+    if (k == 2) return fmaf(t[2], t[3], t[0] * (t[3] * u[2] + t[1] * u[3]));
+    return fmaf(u[0], fmaf(u[1], t[2], t[1]), t[0]);
+}
+
 constexpr int kVolShift = 56;  // fixed point of 6x piece volumes (each <= 6)
 
 ADECO_HD inline long long vol_fixed(float v6)
@@ -154,7 +210,7 @@ ADECO_HD inline float piece_vol6(const float p[12])
 
 // state of one piece: next face to examine -> (code, face); code 0 = dropped,
 // 1 = finished, 2 = split at `face` with inside mask `mask`
-ADECO_HD inline int piece_step(const float p[12], int face0, int &face, int &mask)
+ADECO_HD inline int piece_step(const float p[12], int face0, int &face, int &mask, bool *last = nullptr)
 {
     const int b0 = face_bits(p[0], p[1], p[2]), b1 = face_bits(p[3], p[4], p[5]);
     const int b2 = face_bits(p[6], p[7], p[8]), b3 = face_bits(p[9], p[10], p[11]);
@@ -169,12 +225,13 @@ ADECO_HD inline int piece_step(const float p[12], int face0, int &face, int &mas
     face = __builtin_ctz(next);
 #endif
     mask = ((b0 >> face) & 1) | (((b1 >> face) & 1) << 1) | (((b2 >> face) & 1) << 2) | (((b3 >> face) & 1) << 3);
+    if (last) *last = (next >> (face + 1)) == 0;
     return 2;
 }
 
 // Serial clipping of one piece from face `face0` on (used when the warp pool
-// is full, and by the host model): depth-first over the same splits, so the
-// fixed-point sum is identical to the warp engine's.
+// is full): depth-first over the same splits and last-face fractions, so the
+// fixed-point sum is the warp engine's.
 #ifdef __CUDA_ARCH__
 __device__ __noinline__
 #else
@@ -182,7 +239,7 @@ inline
 #endif
 long long clip_piece_serial(const float p0[12], int face0)
 {
-    constexpr int kDepth = 16;  // 2 pending siblings per face level + 3
+    constexpr int kDepth = 16;  // 2 pending pieces per face level + 3
     float stk[kDepth][12];
     int sface[kDepth];
 #pragma unroll
@@ -196,70 +253,111 @@ long long clip_piece_serial(const float p0[12], int face0)
 #pragma unroll
         for (int x = 0; x < 12; ++x) p[x] = stk[sp][x];
         int face = 0, mask = 0;
-        const int code = piece_step(p, sface[sp], face, mask);
+        bool last = false;
+        const int code = piece_step(p, sface[sp], face, mask, &last);
         if (code == 0) continue;
-        if (code == 1) {
-            acc += vol_fixed(piece_vol6(p));
+        if (code == 1 || last) {
+            acc += vol_fixed(piece_vol6(p) * (code == 1 ? 1.f : inside_fraction(p, mask, face)));
             continue;
         }
         float c0[12], c1[12], c2[12];
         const int n = split_piece(p, mask, face, c0, c1, c2);
-        if (sp + n > kDepth) continue;  // cannot happen (depth <= 2*5 + 3)
+        if (sp + 3 > kDepth) continue;  // cannot happen (depth <= 2*5 + 3)
 #pragma unroll
         for (int x = 0; x < 12; ++x) stk[sp][x] = c0[x];
-        sface[sp++] = face + 1;
+        sface[sp] = face + 1;
+        ++sp;
         if (n == 3) {
 #pragma unroll
             for (int x = 0; x < 12; ++x) stk[sp][x] = c1[x];
-            sface[sp++] = face + 1;
+            sface[sp] = face + 1;
+            ++sp;
 #pragma unroll
             for (int x = 0; x < 12; ++x) stk[sp][x] = c2[x];
-            sface[sp++] = face + 1;
+            sface[sp] = face + 1;
+            ++sp;
         }
     }
     return acc;
 }
 
 #ifdef __CUDACC__
-constexpr int kPool = 64;  // pieces per warp pool
+constexpr int kPool = 64;    // pieces per warp pool
+constexpr int kPairs = 128;  // partial pairs per warp list
 
 struct WarpPool {
     float v[12][kPool];
-    uint32_t meta[kPool];   // owner lane | next face << 8
-    long long vacc[32];     // 6x volume of each pair of the batch, fixed point 2^kVolShift
+    uint32_t meta[kPool];     // owner | face << 8
+    long long vacc[kPairs];   // 6x volume of each listed pair, fixed point 2^kVolShift
 };
 
-// Clip the warp's batch: lane l < nb holds piece p (pair l) on entry.  On
-// return pool.vacc[l] is the exact-sum 6x volume of pair l.  `fallbacks`
-// counts pieces clipped serially because the pool was full.
-__device__ __forceinline__ void clip_batch(WarpPool &pool, float p[12], int nb, unsigned &fallbacks)
+// Clip the warp's list of np partial pairs: an idle lane takes a piece from
+// the pool (last in, first out) or, when the pool is empty, the next pair of
+// the list (build(j, p) writes its tet in cell coordinates).  Each step a
+// lane makes at most one split: at the piece's last crossed face the
+// children are summed in place, otherwise one child is kept and the others
+// pushed.  On return pool.vacc[0..np) hold the pairs' 6x volumes.
+template <typename Build>
+__device__ __forceinline__ void clip_pairs(WarpPool &pool, int np, Build build, unsigned &fallbacks)
 {
     const int lane = threadIdx.x & 31;
-    bool valid = lane < nb;
-    int owner = lane, face = 0;
-    pool.vacc[lane] = 0;
+    const unsigned lt = (1u << lane) - 1;
+    for (int j = lane; j < np; j += 32) pool.vacc[j] = 0;
     __syncwarp();
-    int top = 0;
+    bool valid = false;
+    float p[12];
+    int owner = 0, face = 0;
+    int top = 0, next = 0;
     for (;;) {
+        // refill idle lanes
+        const unsigned need = __ballot_sync(0xffffffffu, !valid);
+        const int rank = __popc(need & lt), nneed = __popc(need);
+        if (!valid) {
+            if (rank < top) {
+                const int idx = top - 1 - rank;
+#pragma unroll
+                for (int x = 0; x < 12; ++x) p[x] = pool.v[x][idx];
+                const uint32_t m = pool.meta[idx];
+                owner = (int)(m & 0xff);
+                face = (int)(m >> 8);
+                valid = true;
+            } else {
+                const int j = next + rank - top;
+                if (j < np) {
+                    build(j, p);
+                    owner = j;
+                    face = 0;
+                    valid = true;
+                }
+            }
+        }
+        const int from_pool = nneed < top ? nneed : top;
+        top -= from_pool;
+        next = min(np, next + (nneed - from_pool));
+        if (!__any_sync(0xffffffffu, valid)) break;
+        __syncwarp();
+        // one step
         int npush = 0;
         float c1[12], c2[12];
         if (valid) {
             int f = 0, mask = 0;
-            const int code = piece_step(p, face, f, mask);
-            if (code == 0) {
-                valid = false;
-            } else if (code == 1) {
-                atomicAdd(reinterpret_cast<unsigned long long *>(&pool.vacc[owner]),
-                          (unsigned long long)vol_fixed(piece_vol6(p)));
-                valid = false;
-            } else {
+            bool last = false;
+            const int code = piece_step(p, face, f, mask, &last);
+            long long v = 0;
+            if (code == 2 && !last) {
                 float c0[12];
                 const int n = split_piece(p, mask, f, c0, c1, c2);
 #pragma unroll
                 for (int x = 0; x < 12; ++x) p[x] = c0[x];
-                face = f + 1;
                 npush = n - 1;
+                face = f + 1;
+            } else {
+                // finished, or at its last crossed face: the inside part
+                // needs no more clipping, so its volume is added here
+                if (code != 0) v = vol_fixed(piece_vol6(p) * (code == 1 ? 1.f : inside_fraction(p, mask, f)));
+                valid = false;
             }
+            if (v) atomicAdd(reinterpret_cast<unsigned long long *>(&pool.vacc[owner]), (unsigned long long)v);
         }
         // push the extra pieces (warp-wide exclusive scan of npush)
         int incl = npush;
@@ -272,15 +370,16 @@ __device__ __forceinline__ void clip_batch(WarpPool &pool, float p[12], int nb, 
         if (total) {
             if (top + total <= kPool) {
                 const int base = top + incl - npush;
+                const uint32_t m = (uint32_t)owner | ((uint32_t)face << 8);
                 if (npush >= 1) {
 #pragma unroll
                     for (int x = 0; x < 12; ++x) pool.v[x][base] = c1[x];
-                    pool.meta[base] = (uint32_t)owner | ((uint32_t)face << 8);
+                    pool.meta[base] = m;
                 }
                 if (npush == 2) {
 #pragma unroll
                     for (int x = 0; x < 12; ++x) pool.v[x][base + 1] = c2[x];
-                    pool.meta[base + 1] = (uint32_t)owner | ((uint32_t)face << 8);
+                    pool.meta[base + 1] = m;
                 }
                 top += total;
             } else if (npush) {  // pool full: finish this lane's extra pieces serially
@@ -291,22 +390,6 @@ __device__ __forceinline__ void clip_batch(WarpPool &pool, float p[12], int nb, 
             }
         }
         __syncwarp();
-        // idle lanes take pieces from the pool, last in first out
-        const unsigned need = __ballot_sync(0xffffffffu, !valid);
-        const int rank = __popc(need & ((1u << lane) - 1));
-        const int nneed = __popc(need);
-        if (!valid && rank < top) {
-            const int idx = top - 1 - rank;
-#pragma unroll
-            for (int x = 0; x < 12; ++x) p[x] = pool.v[x][idx];
-            const uint32_t m = pool.meta[idx];
-            owner = (int)(m & 0xff);
-            face = (int)(m >> 8);
-            valid = true;
-        }
-        top -= (nneed < top) ? nneed : top;
-        __syncwarp();
-        if (!__any_sync(0xffffffffu, valid)) break;
     }
     __syncwarp();
 }

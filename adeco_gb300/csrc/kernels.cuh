@@ -26,7 +26,7 @@ constexpr int kThreads = 128;
 constexpr int kWarps = kThreads / 32;
 constexpr int kMaxVerts = 512;   // 8^3
 constexpr int kMaxCubes = 343;   // 7^3
-constexpr int kQueue = 64;
+constexpr int kQueue = kPairs;  // partial pairs listed per warp before clipping
 
 struct Item {
     long long base;  // vertex index of the block origin (lattice) or of the patch origin + offset
@@ -70,9 +70,7 @@ struct WarpTets {
     float qlo[12][32];   // rounding remainders: q + qlo carries the FP64 vertex
     float n[4][3][32];   // inward face normals
     float d[4][32];      // plane offsets: inside <=> n.x - d > 0
-    float pos[4][32];    // sum of positive normal components
-    float neg[4][32];    // sum of negative normal components
-    float tol[4][32];    // FP32 error bound of the plane test
+    float tol[32];       // FP32 error bound of the plane tests (largest face)
     float bmin[3][32];   // tet AABB in the anchor frame
     float bmax[3][32];
     double factor6[32];  // mass per unit of 6x clipped volume (FP64)
@@ -255,6 +253,7 @@ ADECO_HD inline int setup_tet(const float3 vin[4], const float ghin[4][3], const
 #pragma unroll
         for (int a = 0; a < 3; ++a) R = fmaxf(R, fabsf(qf[q][a]));
     R = fmaxf(R, (float)max(max(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]) + 1.f);
+    float tolmax = 0.f;
 #pragma unroll
     for (int f = 0; f < 4; ++f) {
         // n_in = (vb - va) x (vc - va) with the outward order reversed
@@ -268,13 +267,12 @@ ADECO_HD inline int setup_tet(const float3 vin[4], const float ghin[4][3], const
         W.n[f][1][lane] = ny;
         W.n[f][2][lane] = nz;
         W.d[f][lane] = dd;
-        W.pos[f][lane] = fmaxf(nx, 0.f) + fmaxf(ny, 0.f) + fmaxf(nz, 0.f);
-        W.neg[f][lane] = fminf(nx, 0.f) + fminf(ny, 0.f) + fminf(nz, 0.f);
         const float L1 = fmaxf(fmaxf(fabsf(e1x), fabsf(e1y)), fabsf(e1z));
         const float L2 = fmaxf(fmaxf(fabsf(e2x), fabsf(e2y)), fabsf(e2z));
         // generous bound on the FP32 rounding of n.x - d (|x| <= R + 1)
-        W.tol[f][lane] = 1.0e-5f * L1 * L2 * (R + 1.f);
+        tolmax = fmaxf(tolmax, 1.0e-5f * L1 * L2 * (R + 1.f));
     }
+    W.tol[lane] = tolmax;
 #pragma unroll
     for (int q = 0; q < 4; ++q)
 #pragma unroll
@@ -444,12 +442,14 @@ ADECO_HD inline int classify_pair(const WarpTets &W, const GridDesc &g, int s, i
         W.bmin[2][s] >= fc && W.bmax[2][s] <= fc + 1.f)
         return P_TET_INSIDE;
     bool all_in = true, unsure = false;
+    const float t = W.tol[s];
 #pragma unroll
     for (int f = 0; f < 4; ++f) {
-        const float base = fmaf(W.n[f][0][s], fa, fmaf(W.n[f][1][s], fb, fmaf(W.n[f][2][s], fc, -W.d[f][s])));
-        const float mx = base + W.pos[f][s];
-        const float mn = base + W.neg[f][s];
-        const float t = W.tol[f][s];
+        const float nx = W.n[f][0][s], ny = W.n[f][1][s], nz = W.n[f][2][s];
+        const float base = fmaf(nx, fa, fmaf(ny, fb, fmaf(nz, fc, -W.d[f][s])));
+        const float pos = fmaxf(nx, 0.f) + fmaxf(ny, 0.f) + fmaxf(nz, 0.f);
+        const float mx = base + pos;
+        const float mn = base + ((nx + ny + nz) - pos);
         if (mx < -t) return P_NO;
         if (mx <= t) unsure = true;
         if (mn > t) continue;
@@ -493,18 +493,24 @@ __device__ __forceinline__ void pair_piece(const GridDesc &g, const WarpTets &W,
     }
 }
 
-// clip the nb queued pairs Q[tail..tail+nb) with the whole warp and scatter
-__device__ __forceinline__ void clip_queue(const DepositParams &P, const GridDesc &g, const WarpTets &W,
-                                           WarpPool &pool, const uint32_t *Q, int tail, int nb, unsigned &fallbacks)
+// clip the warp's listed partial pairs Q[0..np), then scatter them
+__device__ __forceinline__ void clip_list(const DepositParams &P, const GridDesc &g, const WarpTets &W,
+                                          WarpPool &pool, const uint32_t *Q, int np, unsigned &fallbacks)
 {
-    const int lane = threadIdx.x & 31;
-    float p[12];
-    int s = 0, a = 0, b = 0, c = 0;
-    if (lane < nb) pair_piece(g, W, Q[(tail + lane) & (kQueue - 1)], p, s, a, b, c);
-    clip_batch(pool, p, nb, fallbacks);
-    if (lane < nb) {
-        const double v6 = ldexp((double)pool.vacc[lane], -kVolShift);
-        const double dm = v6 * W.factor6[s];
+    clip_pairs(
+        pool, np,
+        [&](int j, float *p) {
+            int s, a, b, c;
+            pair_piece(g, W, Q[j], p, s, a, b, c);
+        },
+        fallbacks);
+    for (int j = threadIdx.x & 31; j < np; j += 32) {
+        const uint32_t e = Q[j];
+        const int s = e >> 27;
+        const int local = e & ((1u << 27) - 1);
+        const int ex0 = W.ex[0][s], ex1 = W.ex[1][s];
+        const int a = local % ex0, r = local / ex0, b = r % ex1, c = r / ex1;
+        const double dm = ldexp((double)pool.vacc[j], -kVolShift) * W.factor6[s];
         if (dm > 0.0) scatter(P, g, W, s, a, b, c, dm);
     }
     __syncwarp();
@@ -586,8 +592,14 @@ __global__ void __launch_bounds__(kThreads, 3) deposit_mixed_kernel(DepositParam
             const int total = __shfl_sync(0xffffffffu, incl, 31);
             if (lane == 31) W.scan[32] = total;
             __syncwarp();
-            int head = 0, tail = 0;
-            for (int pb = 0; pb < total; pb += 32) {
+            int np = 0;  // partial pairs listed in Q
+            for (int pb = 0;; pb += 32) {
+                // one call site keeps a single copy of the clip engine
+                if (np > kQueue - 32 || (pb >= total && np)) {
+                    clip_list(P, g, W, pool, Q, np, st_fb);
+                    np = 0;
+                }
+                if (pb >= total) break;
                 const int pidx = pb + lane;
                 bool part = false;
                 uint32_t entry = 0;
@@ -619,15 +631,10 @@ __global__ void __launch_bounds__(kThreads, 3) deposit_mixed_kernel(DepositParam
                     }
                 }
                 const unsigned bal = __ballot_sync(0xffffffffu, part);
-                if (part) Q[(head + __popc(bal & ((1u << lane) - 1))) & (kQueue - 1)] = entry;
-                head += __popc(bal);
+                if (part) Q[np + __popc(bal & ((1u << lane) - 1))] = entry;
+                np += __popc(bal);
                 __syncwarp();
-                if (head - tail >= 32) {
-                    clip_queue(P, g, W, pool, Q, tail, 32, st_fb);
-                    tail += 32;
-                }
             }
-            if (head > tail) clip_queue(P, g, W, pool, Q, tail, head - tail, st_fb);
             // ill-conditioned tets of this group: whole warp, FP64
             while (fp64_tets) {
                 const int src = __ffs(fp64_tets) - 1;
