@@ -327,6 +327,13 @@ def run_ours(args, rank, ws, local):
             err["max_abs_tet_masses"] = float(d.max())
             err["cells_nonzero"] = int((pg > 0).sum())
             err["bar_1e-5_rel_plus_1e-7_abs_ok"] = bool(np.all(d <= 1e-5 * pg + 1e-7))
+            # smallest absolute floor (tet masses) with which every cell meets 1e-5 relative
+            excess = (d - 1e-5 * pg).ravel()
+            worst = int(np.argmax(excess))
+            err["abs_floor_needed_tet_masses"] = float(max(excess[worst], 0.0))
+            err["worst_cell"] = {"fp64": float(pg.flat[worst]), "abs_err": float(d.flat[worst])}
+            for fl in (1e-7, 1e-6):
+                err[f"cells_over_1e-5_rel_plus_{fl:g}"] = int((excess > fl).sum())
             plain["mixed_vs_fp64"] = err
             plain["total_mass_rel_diff"] = abs(mixed_total - float(pg.sum())) / float(pg.sum())
             del pg
