@@ -17,6 +17,7 @@ HEADER = os.path.join(ROOT, "include", "adeco_deposit.h")
 OK = 0
 STATUS_NAMES = {0: "OK", 1: "ERR_ARGUMENT", 2: "ERR_OVERFLOW", 3: "ERR_DEVICE", 4: "ERR_CUDA", 5: "ERR_MEMORY",
                 6: "ERR_INCONSISTENT", 7: "ERR_STATE", 8: "ERR_NOT_FOUND", 9: "ERR_LIMIT"}
+ERR_MEMORY = 5
 PREC_MIXED, PREC_FP64 = 0, 1
 ORDER_REF, ORDER_CONFORMING = 0, 1
 OUT_F32, OUT_F64 = 0, 1
@@ -90,6 +91,7 @@ _SIGS = {
     "adeco_session_wait": ([_vp, C.c_uint64, _d], _i),
     "adeco_session_result": ([_vp, C.c_uint64, _i, _vp, _sz], _i),
     "adeco_session_latency": ([_vp, C.c_uint64, _i, C.POINTER(_d)], _i),
+    "adeco_session_batch_device_ms": ([_vp, C.c_uint64, C.POINTER(C.c_double)], _i),
     "adeco_session_release": ([_vp, C.c_uint64], _i),
     "adeco_debug_tet_records": ([_vp, _sz, _i, _sz, _sz, _vp, _i, _i, _vp, _vp], _i),
     "adeco_probe_fp32_tflops": ([_i, C.POINTER(_d)], _i),

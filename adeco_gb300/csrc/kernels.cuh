@@ -165,7 +165,7 @@ __device__ __forceinline__ bool cube_alive(const float4 *vert, int vx, int vy, i
     if (pad) return false;
 #pragma unroll
     for (int a = 0; a < 3; ++a)
-        if (!(mn[a] < g.gmax[a] && g.gmin[a] < mx[a])) return false;
+        if (!(mn[a] < g.cull_max[a] && g.cull_min[a] < mx[a])) return false;
     return true;
 }
 
@@ -202,6 +202,7 @@ ADECO_HD inline int setup_tet(const float3 vin[4], const float ghin[4][3], const
     int lo[3], hi[3];
     if (!candidate_range(v, g, lo, hi)) return 0;
     if (sgn == 0) return 0;
+    if (!tile_clamp(g, lo, hi)) return 0;
     {
         const long long cnt0 = (long long)(hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
         if (cnt0 > kMaxPairsPerTet) {
@@ -648,7 +649,7 @@ __global__ void __launch_bounds__(kThreads, 3) deposit_mixed_kernel(DepositParam
                     v[3] = t;
                 }
                 int lo[3], hi[3];
-                candidate_range(v, g, lo, hi);
+                if (!candidate_range(v, g, lo, hi) || !tile_clamp(g, lo, hi)) continue;
                 unsigned c64 = 0, p64 = 0;
                 deposit_tet_fp64_warp<true>(v, lo, hi, g, P.out, nullptr, c64, p64);
                 st_cand += c64;
@@ -723,7 +724,7 @@ __global__ void __launch_bounds__(kThreads) deposit_plain_fp64_kernel(DepositPar
             const float v6 = vol6_exact(v[0], v[1], v[2], v[3]);
             const int sgn = vol6_sign_ref(v6);
             int lo[3], hi[3];
-            if (!candidate_range(v, g, lo, hi) || sgn == 0) continue;
+            if (!candidate_range(v, g, lo, hi) || sgn == 0 || !tile_clamp(g, lo, hi)) continue;
             if (sgn < 0) { const float3 tt = v[0]; v[0] = v[3]; v[3] = tt; }
             unsigned nc = 0, np = 0;
             deposit_tet_fp64_warp<false>(v, lo, hi, g, nullptr, P.out_d, nc, np);

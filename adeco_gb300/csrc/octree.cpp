@@ -3,6 +3,7 @@
 #include "octree.h"
 
 #include <algorithm>
+#include <cmath>
 
 namespace adeco {
 
@@ -140,6 +141,79 @@ bool Octree::build(const MetaGrid &mg, const float box6[6], const float roi6[6],
     }
     leaf_meta_off.push_back(off);
     return true;
+}
+
+void MetaIndex::build(const MetaGrid &mg)
+{
+    const uint64_t n = mg.count();
+    float hi[3] = {0, 0, 0};
+    double ext[3] = {0, 0, 0};
+    for (int a = 0; a < 3; ++a) {
+        lo[a] = n ? mg.bbox[a] : 0.f;
+        hi[a] = n ? mg.bbox[3 + a] : 0.f;
+    }
+    for (uint64_t id = 0; id < n; ++id) {
+        const float *b = &mg.bbox[6 * id];
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = std::min(lo[a], b[a]);
+            hi[a] = std::max(hi[a], b[3 + a]);
+            ext[a] += (double)b[3 + a] - (double)b[a];
+        }
+    }
+    // buckets about twice a meta-cell's mean extent, at most 64 per axis
+    for (int a = 0; a < 3; ++a) {
+        const double span = std::max((double)hi[a] - (double)lo[a], 1e-30);
+        const double want = n ? 2.0 * ext[a] / (double)n : span;
+        nb[a] = (int)std::min(64.0, std::max(1.0, std::floor(span / std::max(want, 1e-30))));
+        inv[a] = (float)(nb[a] / span);
+    }
+    const size_t nbk = (size_t)nb[0] * nb[1] * nb[2];
+    start.assign(nbk + 1, 0);
+    std::vector<uint32_t> fill;
+    for (int pass = 0; pass < 2; ++pass) {
+        if (pass == 1) {
+            for (size_t k = 0; k < nbk; ++k) start[k + 1] += start[k];
+            ids.assign(start[nbk], 0);
+            fill.assign(start.begin(), start.end() - 1);
+        }
+        for (uint64_t id = 0; id < n; ++id) {
+            const float *b = &mg.bbox[6 * id];
+            int r[6];
+            for (int a = 0; a < 3; ++a) {
+                r[a] = std::max(0, std::min(nb[a] - 1, (int)((b[a] - lo[a]) * inv[a])));
+                r[3 + a] = std::max(0, std::min(nb[a] - 1, (int)((b[3 + a] - lo[a]) * inv[a])));
+            }
+            for (int z = r[2]; z <= r[5]; ++z)
+                for (int y = r[1]; y <= r[4]; ++y)
+                    for (int x = r[0]; x <= r[3]; ++x) {
+                        const size_t k = (size_t)x + (size_t)nb[0] * ((size_t)y + (size_t)nb[1] * z);
+                        if (pass == 0)
+                            ++start[k + 1];
+                        else
+                            ids[fill[k]++] = (uint32_t)id;
+                    }
+        }
+    }
+    built = true;
+}
+
+void MetaIndex::query(const MetaGrid &mg, const float box6[6], std::vector<uint32_t> &out) const
+{
+    out.clear();
+    int r[6];
+    for (int a = 0; a < 3; ++a) {
+        r[a] = std::max(0, std::min(nb[a] - 1, (int)((box6[a] - lo[a]) * inv[a])));
+        r[3 + a] = std::max(0, std::min(nb[a] - 1, (int)((box6[3 + a] - lo[a]) * inv[a])));
+    }
+    for (int z = r[2]; z <= r[5]; ++z)
+        for (int y = r[1]; y <= r[4]; ++y)
+            for (int x = r[0]; x <= r[3]; ++x) {
+                const size_t k = (size_t)x + (size_t)nb[0] * ((size_t)y + (size_t)nb[1] * z);
+                for (uint32_t q = start[k]; q < start[k + 1]; ++q)
+                    if (meets(&mg.bbox[6 * (size_t)ids[q]], box6)) out.push_back(ids[q]);
+            }
+    std::sort(out.begin(), out.end());
+    out.erase(std::unique(out.begin(), out.end()), out.end());
 }
 
 }  // namespace adeco

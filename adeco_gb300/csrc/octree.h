@@ -57,6 +57,21 @@ struct OctNode {
     uint64_t estimate;
 };
 
+// Spatial index over the meta-cells' AABBs: a uniform grid of buckets, each
+// listing the meta-cells whose AABB meets it, so that a zoom box visits only
+// the meta-cells near it instead of all of them.
+struct MetaIndex {
+    float lo[3] = {0, 0, 0}, inv[3] = {0, 0, 0};
+    int nb[3] = {0, 0, 0};
+    std::vector<uint32_t> start;  // CSR over the buckets, x fastest
+    std::vector<uint32_t> ids;
+    bool built = false;
+
+    void build(const MetaGrid &mg);
+    // meta-cells whose AABB strictly meets box6 (min xyz, max xyz), ascending
+    void query(const MetaGrid &mg, const float box6[6], std::vector<uint32_t> &out) const;
+};
+
 struct Octree {
     std::vector<OctNode> nodes;
     std::vector<int32_t> leaves;              // getLeafNodes order

@@ -121,6 +121,12 @@ GridDesc make_grid(const float bbox[6], int dims, double tet_mass, int shift, lo
     g.dims = dims;
     g.shift = shift;
     g.out_offset = out_offset;
+    for (int a = 0; a < 3; ++a) {
+        g.tile_lo[a] = 0;
+        g.tile_hi[a] = dims - 1;
+        g.cull_min[a] = g.gmin[a];
+        g.cull_max[a] = g.gmax[a];
+    }
     return g;
 }
 
@@ -453,6 +459,7 @@ struct adeco_session {
     int nx = 0, ny = 0, nz = 0;
     DevBuf<float4> lattice;
     MetaGrid meta;
+    MetaIndex meta_index;  // built at the first zoom batch
     float bbox6[6] = {0, 0, 0, 0, 0, 0};  // xmin,xmax,ymin,ymax,zmin,zmax
     // octree + leaf deposit state
     Octree tree;
@@ -903,11 +910,13 @@ extern "C" int adeco_debug_tet_records(const float *positions, size_t positions_
 // batches submitted while others run overlap on the device.
 struct adeco_session::Batch {
     std::vector<adeco_request> reqs;
-    std::vector<GridDesc> grids;
+    std::vector<GridDesc> grids;     // one per tile of each request
     std::vector<long long> offsets;  // first cell of each request
+    std::vector<int> shifts;         // fixed-point scale of each request
     size_t cells = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
+    cudaEvent_t t0 = nullptr, t1 = nullptr;  // device time of the batch's deposit
     DevBuf<Item> d_items;
     DevBuf<GridDesc> d_grids;
     DevBuf<unsigned long long> d_fixed;
@@ -918,9 +927,13 @@ struct adeco_session::Batch {
     ~Batch()
     {
         if (done) cudaEventDestroy(done);
+        if (t0) cudaEventDestroy(t0);
+        if (t1) cudaEventDestroy(t1);
         if (stream) cudaStreamDestroy(stream);
     }
 };
+
+constexpr int kZoomTile = 64;  // cells per tile edge of a zoom grid
 
 static void request_box(const adeco_request &r, float bb[6])
 {
@@ -944,30 +957,58 @@ extern "C" int adeco_session_submit(adeco_session *s, const adeco_request *reqs,
     b->t_submit = std::chrono::steady_clock::now();
     b->reqs.assign(reqs, reqs + n);
     std::vector<Item> items;
+    std::vector<uint32_t> hits;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (!s->meta_index.built) s->meta_index.build(s->meta);
+    }
     long long off = 0;
     for (int i = 0; i < n; ++i) {
         float bb[6];
         request_box(reqs[i], bb);
-        const float box6[6] = {bb[0], bb[2], bb[4], bb[1], bb[3], bb[5]};
-        const int grid_index = i;
-        size_t first = items.size();
-        for (uint64_t id = 0; id < s->meta.count(); ++id) {
-            const float *m = &s->meta.bbox[6 * id];
-            if (!(m[0] < box6[3] && box6[0] < m[3] && m[1] < box6[4] && box6[1] < m[4] && m[2] < box6[5] &&
-                  box6[2] < m[5]))
-                continue;
-            int org[3], nv[3];
-            s->meta.range(id, org, nv);
-            Item it;
-            it.base = org[0] + (long long)s->nx * (org[1] + (long long)s->ny * org[2]);
-            it.grid = grid_index;
-            it.nv = nv[0] | (nv[1] << 8) | (nv[2] << 16);
-            items.push_back(it);
-        }
+        const int d = reqs[i].dims;
+        const GridDesc g0 = make_grid(bb, d, s->tet_mass, 0, off);
+        // Grids larger than kZoomTile^3 cells are split into tiles, one work
+        // item per (tile, meta-cell): when the cells are much smaller than
+        // the tets, a meta-cell's tets cover very many cells, and one work
+        // item per meta-cell would leave all of that to a single CTA.
+        const int nt = (d + kZoomTile - 1) / kZoomTile;
+        const size_t first_grid = b->grids.size(), first = items.size();
+        for (int tz = 0; tz < nt; ++tz)
+            for (int ty = 0; ty < nt; ++ty)
+                for (int tx = 0; tx < nt; ++tx) {
+                    GridDesc gt = g0;
+                    const int t[3] = {tx, ty, tz};
+                    for (int a = 0; a < 3; ++a) {
+                        gt.tile_lo[a] = t[a] * kZoomTile;
+                        gt.tile_hi[a] = std::min(d, (t[a] + 1) * kZoomTile) - 1;
+                        // the tile's world box widened by a cell, inside the grid box
+                        gt.cull_min[a] = std::max(g0.gmin[a], g0.gmin[a] + (float)(gt.tile_lo[a] - 1) * g0.delta[a]);
+                        gt.cull_max[a] = std::min(g0.gmax[a], g0.gmin[a] + (float)(gt.tile_hi[a] + 2) * g0.delta[a]);
+                    }
+                    const float box6[6] = {gt.cull_min[0], gt.cull_min[1], gt.cull_min[2],
+                                           gt.cull_max[0], gt.cull_max[1], gt.cull_max[2]};
+                    s->meta_index.query(s->meta, box6, hits);
+                    if (hits.empty()) continue;
+                    const int grid_index = (int)b->grids.size();
+                    b->grids.push_back(gt);
+                    for (const uint32_t id : hits) {
+                        int org[3], nv[3];
+                        s->meta.range(id, org, nv);
+                        Item it;
+                        it.base = org[0] + (long long)s->nx * (org[1] + (long long)s->ny * org[2]);
+                        it.grid = grid_index;
+                        it.nv = nv[0] | (nv[1] << 8) | (nv[2] << 16);
+                        items.push_back(it);
+                    }
+                }
+        // fixed-point scale from the tets the request can see (all its tiles)
         const double tets = 2058.0 * (double)std::max<size_t>(1, items.size() - first);
-        b->grids.push_back(make_grid(bb, reqs[i].dims, s->tet_mass, choose_shift(tets, s->tet_mass), off));
+        const int shift = choose_shift(tets, s->tet_mass);
+        for (size_t k = first_grid; k < b->grids.size(); ++k) b->grids[k].shift = shift;
+        b->shifts.push_back(shift);
         b->offsets.push_back(off);
-        off += (long long)reqs[i].dims * reqs[i].dims * reqs[i].dims;
+        off += (long long)d * d * d;
     }
     b->cells = (size_t)off;
     b->n_items = (int)items.size();
@@ -984,6 +1025,8 @@ extern "C" int adeco_session_submit(adeco_session *s, const adeco_request *reqs,
         return rc;
     CUDA_TRY(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
     CUDA_TRY(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventCreate(&b->t0));
+    CUDA_TRY(cudaEventCreate(&b->t1));
     CUDA_TRY(cudaMemcpyAsync(b->d_items.p, items.data(), items.size() * sizeof(Item), cudaMemcpyHostToDevice, b->stream));
     CUDA_TRY(cudaMemcpyAsync(b->d_grids.p, b->grids.data(), b->grids.size() * sizeof(GridDesc), cudaMemcpyHostToDevice,
                              b->stream));
@@ -1002,7 +1045,9 @@ extern "C" int adeco_session_submit(adeco_session *s, const adeco_request *reqs,
     P.out = b->d_fixed.p;
     P.counter = b->d_counter.p;
     P.error = b->d_counter.p + 1;
+    CUDA_TRY(cudaEventRecord(b->t0, b->stream));
     if ((rc = launch_mixed(s->dp, P, s->acc_fp64, b->stream))) return rc;
+    CUDA_TRY(cudaEventRecord(b->t1, b->stream));
     CUDA_TRY(cudaEventRecord(b->done, b->stream));
     std::lock_guard<std::mutex> lk(s->mu);
     *batch_id = s->next_batch++;
@@ -1075,7 +1120,7 @@ extern "C" int adeco_session_result(adeco_session *s, uint64_t batch_id, int ind
     std::vector<unsigned long long> tmp(n);
     CUDA_TRY(cudaMemcpy(tmp.data(), b->d_fixed.p + b->offsets[index], n * sizeof(unsigned long long),
                         cudaMemcpyDeviceToHost));
-    const double scale = std::ldexp(1.0, -b->grids[index].shift);
+    const double scale = std::ldexp(1.0, -b->shifts[index]);
     for (size_t c = 0; c < n; ++c) host_out[c] = (double)tmp[c] * scale;
     return ADECO_OK;
 }
@@ -1088,6 +1133,19 @@ extern "C" int adeco_session_latency(adeco_session *s, uint64_t batch_id, int in
     if (index < 0 || index >= (int)b->reqs.size()) return fail(ADECO_ERR_ARGUMENT, "request index out of range");
     if (b->latency_ms < 0) return fail(ADECO_ERR_STATE, "batch not finished");
     *ms = b->latency_ms;
+    return ADECO_OK;
+}
+
+extern "C" int adeco_session_batch_device_ms(adeco_session *s, uint64_t batch_id, double *ms)
+{
+    if (!s || !ms) return fail(ADECO_ERR_ARGUMENT, "null argument");
+    auto b = find_batch(s, batch_id);
+    if (!b) return fail(ADECO_ERR_NOT_FOUND, "unknown batch %llu", (unsigned long long)batch_id);
+    int rc = adeco_session_wait(s, batch_id, 3600.0);
+    if (rc) return rc;
+    float f = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&f, b->t0, b->t1));
+    *ms = f;
     return ADECO_OK;
 }
 

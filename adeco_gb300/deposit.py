@@ -236,6 +236,12 @@ class Session:
         _raise(self._lib.adeco_session_latency(self._h, C.c_uint64(batch), int(index), C.byref(v)))
         return v.value
 
+    def device_ms(self, batch):
+        """Device time of the batch's deposit launch (waits for the batch)."""
+        v = C.c_double()
+        _raise(self._lib.adeco_session_batch_device_ms(self._h, C.c_uint64(batch), C.byref(v)))
+        return v.value
+
     def release(self, batch):
         _raise(self._lib.adeco_session_release(self._h, C.c_uint64(batch)))
 

@@ -210,6 +210,8 @@ int adeco_session_wait(adeco_session *s, uint64_t batch_id, double timeout_s);
 int adeco_session_result(adeco_session *s, uint64_t batch_id, int index, double *host_out, size_t capacity);
 /* latency (submit -> done, host clock) of request `index`, milliseconds */
 int adeco_session_latency(adeco_session *s, uint64_t batch_id, int index, double *ms);
+/* device time of the batch's deposit launch (CUDA events on its stream), milliseconds; waits for the batch */
+int adeco_session_batch_device_ms(adeco_session *s, uint64_t batch_id, double *ms);
 int adeco_session_release(adeco_session *s, uint64_t batch_id);
 
 /* ------------------------------------------------------------------ */

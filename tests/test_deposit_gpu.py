@@ -1,7 +1,7 @@
 """GPU parity: the CUDA path (through the C ABI) against the oracle and the
 reference-made golden fixtures.
 
-Bars (see DESIGN.md "Parity"):
+Bars:
 * tet connectivity and per-tet candidate ranges / per-cell candidate counts:
   bit-exact;
 * octree topology: bit-exact;
