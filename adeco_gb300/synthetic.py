@@ -59,17 +59,33 @@ def zeldovich_lattice(n: int, L: float = 100.0, seed: int = 0, rms_disp: float =
 
 def _apply_infall(pos, n, L, count, seed, concentration=10.0):
     """Spherical infall regions: centres uniform, radii log-uniform in
-    [0.5, 5] lattice spacings, NFW-like radial compression."""
+    [0.5, 5] lattice spacings, NFW-like radial compression of the particles
+    within 3 radii of the centre.  A region looks at the lattice sites within
+    (3 radii + the largest displacement so far) of its centre, so the cost is
+    local; the regions are applied in order."""
     rng = np.random.default_rng(seed + 1000003)
     spacing = L / n
     centres = rng.uniform(0.0, L, size=(count, 3))
     radii = np.exp(rng.uniform(np.log(0.5), np.log(5.0), size=count)) * spacing
-    flat = pos.reshape(-1, 3)
+    q1 = (np.arange(n) + 0.5) * spacing
+    disp = 0.0
+    for a, sl in enumerate((np.s_[None, None, :], np.s_[None, :, None], np.s_[:, None, None])):
+        d = pos[..., a] - q1[sl]
+        d -= L * np.round(d / L)
+        disp = max(disp, float(np.abs(d).max()))
     for c, r in zip(centres, radii):
         reach = 3.0 * r
-        d = flat - c
+        w = reach + disp
+        idx = []
+        for a in range(3):
+            lo = int(np.floor((c[a] - w) / spacing)) - 1
+            hi = int(np.ceil((c[a] + w) / spacing)) + 1
+            idx.append(np.arange(n) if hi - lo + 1 >= n else np.arange(lo, hi + 1) % n)
+        win = np.ix_(idx[2], idx[1], idx[0])
+        sub = pos[win]
+        d = sub - c
         d -= L * np.round(d / L)
-        dist = np.sqrt(np.sum(d * d, axis=1))
+        dist = np.sqrt(np.sum(d * d, axis=-1))
         sel = dist < reach
         if not np.any(sel):
             continue
@@ -78,7 +94,42 @@ def _apply_infall(pos, n, L, count, seed, concentration=10.0):
         g = np.log1p(concentration * x) / np.log1p(concentration)
         new = reach * (x * 0.5 + 0.5 * g * x)
         scale = np.where(dist[sel] > 0, new / np.maximum(dist[sel], 1e-12), 1.0)
-        flat[sel] = c + d[sel] * scale[:, None]
+        moved = c + d[sel] * scale[:, None]
+        site = np.stack(np.broadcast_arrays(q1[idx[0]][None, None, :], q1[idx[1]][None, :, None],
+                                            q1[idx[2]][:, None, None]), axis=-1)[sel]
+        dq = moved - site
+        dq -= L * np.round(dq / L)
+        disp = max(disp, float(np.abs(dq).max()))
+        sub[sel] = moved
+        pos[win] = sub
+
+
+def zoom_requests(count: int = 512, L: float = 100.0, seed: int = 1, side=(0.01, 0.25),
+                  dims=(32, 64, 128, 256)):
+    """Zoom requests (centre, side, dims): centres uniform in the box, sides
+    log-uniform in side * L, resolution drawn uniformly from `dims`."""
+    rng = np.random.default_rng(seed)
+    centres = rng.uniform(0.0, L, size=(count, 3))
+    sides = L * np.exp(rng.uniform(np.log(side[0]), np.log(side[1]), size=count))
+    res = rng.choice(np.asarray(dims), size=count)
+    return [(tuple(float(v) for v in c), float(s_), int(d)) for c, s_, d in zip(centres, sides, res)]
+
+
+def poisson_requests(rate: float, duration_s: float, L: float = 100.0, seed: int = 2, side=(0.005, 0.5),
+                     dims=(32, 64, 128, 256, 512)):
+    """Serving stream: Poisson arrivals at `rate` per second over `duration_s`;
+    each request a zoom box (side log-uniform in side * L, resolution drawn
+    uniformly from `dims`).  Returns [(arrival_s, (centre, side, dims))]."""
+    rng = np.random.default_rng(seed)
+    out, t = [], 0.0
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= duration_s:
+            return out
+        c = rng.uniform(0.0, L, size=3)
+        s_ = L * np.exp(rng.uniform(np.log(side[0]), np.log(side[1])))
+        d = int(rng.choice(np.asarray(dims)))
+        out.append((t, (tuple(float(v) for v in c), float(s_), d)))
 
 
 def periodic_ghost_lattice(pos: np.ndarray, L: float) -> np.ndarray:

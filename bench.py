@@ -40,11 +40,15 @@ sys.path.insert(0, ROOT)
 N_PART = 256
 L_BOX = 100.0
 RMS_DISP = 3.0
+SEED = 0
+INFALL = 0
 MAX_TETS = 64 * 16 ** 3
 MAX_LEVEL = 8
 LEAF = 16
 WORKLOAD = ("octree deposit of a 256^3 Zel'dovich lattice (rms disp 3 spacings, seed 0, L=100): "
             "depth <= 8, 16^3-cell leaves, refine while tet estimate > 262144 (64 per cell)")
+ZOOM_COUNT, ZOOM_SEED = 512, 1
+SERVE_SEED = 2
 
 
 def dist_env():
@@ -148,13 +152,24 @@ class ClockSampler:
 
 def workload_positions():
     from adeco_gb300.synthetic import zeldovich_lattice
-    return zeldovich_lattice(N_PART, L=L_BOX, seed=0, rms_disp=RMS_DISP)
+    return zeldovich_lattice(N_PART, L=L_BOX, seed=SEED, rms_disp=RMS_DISP, infall=INFALL)
 
 
 def set_size(n):
     """Lattice size (256 for the benchmark; smaller only for checking this script)."""
     global N_PART
     N_PART = n
+
+
+def set_workload(name):
+    """c2: the benchmark (256^3 octree deposit).  c4: 512^3 lattice with 2000
+    infall regions (seed 4), octree depth <= 12.  zoom and serve run on the c2
+    lattice."""
+    global N_PART, SEED, INFALL, MAX_LEVEL, WORKLOAD
+    if name == "c4":
+        N_PART, SEED, INFALL, MAX_LEVEL = 512, 4, 2000, 12
+        WORKLOAD = ("octree deposit of a 512^3 Zel'dovich lattice with 2000 infall regions (rms disp 3 spacings, "
+                    "seed 4, L=100): depth <= 12, 16^3-cell leaves, refine while tet estimate > 262144")
 
 
 def measured_peaks():
@@ -424,6 +439,105 @@ def run_ours(args, rank, ws, local):
     return 0
 
 
+# --------------------------------------------------------------- zoom batches and serving
+def run_zoom(args, rank, ws, local):
+    """512 zoom requests on the resident 256^3 lattice, one batch (one launch) per step."""
+    from adeco_gb300 import deposit as D
+    from adeco_gb300.synthetic import zoom_requests
+    if rank != 0:
+        return 0
+    pos = workload_positions()
+    reqs = zoom_requests(ZOOM_COUNT, L=L_BOX, seed=ZOOM_SEED, dims=tuple(args.zoom_dims))
+    cells = sum(r[2] ** 3 for r in reqs)
+    dev, host = [], []
+    same = None
+    with D.Session(pos, device=args.device) as s:
+        for step in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            b = s.submit(reqs)
+            s.wait(b)
+            t1 = time.perf_counter()
+            ms = s.device_ms(b)
+            if step == 0:
+                # a request alone gives the same masses as inside the batch
+                k = min(range(len(reqs)), key=lambda i: reqs[i][2])
+                b1 = s.submit([reqs[k]])
+                same = bool(np.array_equal(s.result(b1, 0, reqs[k][2]), s.result(b, k, reqs[k][2])))
+                s.release(b1)
+            s.release(b)
+            if step >= args.warmup:
+                dev.append(ms)
+                host.append((t1 - t0) * 1e3)
+    ms = statistics.median(dev)
+    line = {
+        "metric": "zoom requests/s", "value": len(reqs) / (ms * 1e-3), "unit": "requests/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{len(reqs)} zoom requests (seed {ZOOM_SEED}): centres uniform, side log-uniform "
+                               f"[0.01L, 0.25L], resolution from {args.zoom_dims}, on the 256^3 lattice (seed 0)",
+                   "cells": cells, "batch": "all requests in one batch, one launch per step"},
+        "cells_per_s": cells / (ms * 1e-3),
+        "host_ms_per_batch": statistics.median(host),
+        "alone_equals_in_batch": same,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_serve(args, rank, ws, local):
+    """Poisson stream of zoom requests, one batch per request as it arrives;
+    latency = arrival -> results ready on the device (host clock)."""
+    from adeco_gb300 import _lib as LB
+    from adeco_gb300 import deposit as D
+    from adeco_gb300.synthetic import poisson_requests
+    if rank != 0:
+        return 0
+    pos = workload_positions()
+    stream = poisson_requests(args.serve_rate, args.serve_seconds, L=L_BOX, seed=SERVE_SEED,
+                              dims=tuple(args.serve_dims))
+    lat, refused = [], 0
+    with D.Session(pos, device=args.device) as s:
+        for _, r in stream[:3]:  # warm-up
+            b = s.submit([r])
+            s.wait(b)
+            s.release(b)
+        pending = {}
+        t_start = time.perf_counter()
+        i = 0
+        while i < len(stream) or pending:
+            now = time.perf_counter() - t_start
+            while i < len(stream) and stream[i][0] <= now:
+                try:
+                    pending[s.submit([stream[i][1]])] = stream[i][0]
+                    i += 1
+                except D.AdecoError as e:
+                    if e.code != LB.ERR_MEMORY or not pending:
+                        raise
+                    refused += 1      # admission: no HBM for it now; retry once something finishes
+                    break
+            for b in list(pending):
+                if s.poll(b):
+                    lat.append((time.perf_counter() - t_start - pending.pop(b)) * 1e3)
+                    s.release(b)
+            time.sleep(0.0002)
+        wall = time.perf_counter() - t_start
+    lat = np.sort(np.asarray(lat))
+    line = {
+        "metric": "serving latency p50", "value": float(np.percentile(lat, 50)), "unit": "ms", "n_gpus": 1,
+        "steps": len(lat), "warmup": 3, "ms_per_step": float(np.mean(lat)), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"Poisson arrivals at {args.serve_rate:g} req/s for {args.serve_seconds:g} s "
+                               f"(seed {SERVE_SEED}): zoom boxes, side log-uniform [0.005L, 0.5L], resolution from "
+                               f"{args.serve_dims}, on the 256^3 lattice (seed 0); one batch per request"},
+        "p50_ms": float(np.percentile(lat, 50)), "p90_ms": float(np.percentile(lat, 90)),
+        "p99_ms": float(np.percentile(lat, 99)), "max_ms": float(lat[-1]),
+        "requests": len(lat), "offered_rate": args.serve_rate, "achieved_rate": len(lat) / wall,
+        "admission_retries": refused,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -438,14 +552,25 @@ def main():
     ap.add_argument("--skip-plain", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
-    ap.add_argument("--n", type=int, default=256, help="lattice size; the benchmark workload is 256")
+    ap.add_argument("--n", type=int, default=None, help="lattice size; the benchmark workload is 256")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c4", "zoom", "serve"])
+    ap.add_argument("--zoom-dims", type=int, nargs="+", default=[32, 64, 128, 256])
+    ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--serve-seconds", type=float, default=10.0)
+    ap.add_argument("--serve-dims", type=int, nargs="+", default=[32, 64, 128, 256, 512])
     args = ap.parse_args()
-    set_size(args.n)
+    set_workload(args.workload)
+    if args.n:
+        set_size(args.n)
     if args.warmup < 3:
         args.warmup = 3
     ws, rank, local = dist_env()
     if args.impl == "reference":
         return run_reference(args, rank, ws)
+    if args.workload == "zoom":
+        return run_zoom(args, rank, ws, local)
+    if args.workload == "serve":
+        return run_serve(args, rank, ws, local)
     return run_ours(args, rank, ws, local)
 
 

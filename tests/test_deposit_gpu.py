@@ -247,3 +247,49 @@ def test_zoom_batch_same_alone_and_in_mix(adeco):
         for a, m_ in zip(alone, mixed):
             assert np.array_equal(a, m_)
         assert s.latency_ms(b1, 0) > 0
+
+
+def test_zoom_requests_vs_oracle(adeco, oracle):
+    """Zoom boxes over a resident lattice against the FP64 oracle over the same
+    meta-cells: per-cell bar and total mass, boxes inside, across and beyond
+    the particle distribution, at resolutions from coarse (many tets per cell)
+    to fine (many cells per tet), one grid split into several tiles."""
+    from adeco_gb300.synthetic import zeldovich_lattice
+    n = 22
+    pos = zeldovich_lattice(n, L=40.0, seed=11, rms_disp=2.0)
+    flat = np.ascontiguousarray(pos.reshape(-1))
+    cd = -(-(n - 1) // 7)
+    ids = np.arange(cd ** 3, dtype=np.uint64)
+    reqs = [((20.0, 20.0, 20.0), 12.0, 8), ((8.0, 30.0, 15.0), 7.0, 24), ((38.0, 2.0, 20.0), 9.0, 16),
+            ((21.3, 18.7, 25.1), 2.5, 40), ((19.0, 21.0, 20.5), 6.0, 80)]
+    with adeco.Session(pos) as s:
+        b = s.submit(reqs)
+        s.wait(b)
+        assert s.device_ms(b) > 0
+        for k, (c, side, d) in enumerate(reqs):
+            got = s.result(b, k, d).reshape(-1)
+            h = np.float32(0.5) * np.float32(side)
+            box = np.array([np.float32(c[0]) - h, np.float32(c[0]) + h, np.float32(c[1]) - h, np.float32(c[1]) + h,
+                            np.float32(c[2]) - h, np.float32(c[2]) + h], np.float32)
+            ref = oracle.deposit_meta(flat, (n, n, n), ids, box, d, fp64=True)
+            bad = np.abs(got - ref) > REL * np.abs(ref) + ABS
+            assert not bad.any(), (k, int(bad.sum()), float(np.abs(got - ref).max()))
+            assert abs(got.sum() - ref.sum()) <= 1e-9 * ref.sum() + 3e-7 * np.sqrt(6 * (n - 1) ** 3) + 1e-12
+        s.release(b)
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["mixed", "plain_fp64"])
+def test_fine_grid_vs_oracle(adeco, oracle, precision):
+    """Cells much smaller than the tets (tens of cells per tet edge): same
+    masses as the oracle's cell-by-cell deposit on both paths."""
+    from adeco_gb300.synthetic import zeldovich_lattice
+    n = 8
+    pos = zeldovich_lattice(n, L=16.0, seed=21, rms_disp=1.5)
+    bb = np.array([5.0, 9.0, 5.0, 9.0, 5.0, 9.0], np.float32)
+    dims = 72
+    ref = oracle.deposit_patches(pos.reshape(-1), n - 1, bb, dims, fp64=True)
+    got = adeco.deposit_tets_ex(pos.reshape(-1), n - 1, bb, dims, precision=precision)
+    if precision == 1:
+        assert np.allclose(got, ref, rtol=1e-10, atol=1e-12)
+    else:
+        check_cells(got, ref, n_tets=6 * (n - 1) ** 3)
