@@ -162,13 +162,11 @@ ADECO_HD inline int split_piece(const float p[12], int mask, int f, float c0[12]
 //   k = 3: 1 - u_AD u_BD u_CD = t_AD + u_AD (t_BD + u_BD t_CD)
 // Every term is non-negative, so the fraction carries a few ulps of relative
 // error and the inside volume needs no cut points and no child volumes.
-ADECO_HD inline float inside_fraction(const float p[12], int mask, int f)
+// The same fraction for any linear function over the tet: x0..x3 its values
+// at the vertices, inside = the side of `plane` given by mask.
+ADECO_HD inline float side_fraction(float x0, float x1, float x2, float x3, int mask, float plane)
 {
-    const int axis = f >> 1;
-    const float plane = (f & 1) ? 1.f : 0.f;
     const int pm = split_perm(mask), k = split_kin(mask);
-    const float x0 = sel3(axis, p[0], p[1], p[2]), x1 = sel3(axis, p[3], p[4], p[5]);
-    const float x2 = sel3(axis, p[6], p[7], p[8]), x3 = sel3(axis, p[9], p[10], p[11]);
     const float a = sel4(pm & 3, x0, x1, x2, x3), b = sel4((pm >> 2) & 3, x0, x1, x2, x3);
     const float c = sel4((pm >> 4) & 3, x0, x1, x2, x3), d = sel4((pm >> 6) & 3, x0, x1, x2, x3);
     // edges as in split_piece: k=1: AB AC AD; k=2: AC AD BC BD; k=3: AD BD CD
@@ -193,6 +191,36 @@ ADECO_HD inline float inside_fraction(const float p[12], int mask, int f)
     if (k == 1) return t[0] * t[1] * t[2];
     if (k == 2) return fmaf(t[2], t[3], t[0] * (t[3] * u[2] + t[1] * u[3]));
     return fmaf(u[0], fmaf(u[1], t[2], t[1]), t[0]);
+}
+
+ADECO_HD inline float inside_fraction(const float p[12], int mask, int f)
+{
+    const int axis = f >> 1;
+    const float x0 = sel3(axis, p[0], p[1], p[2]), x1 = sel3(axis, p[3], p[4], p[5]);
+    const float x2 = sel3(axis, p[6], p[7], p[8]), x3 = sel3(axis, p[9], p[10], p[11]);
+    return side_fraction(x0, x1, x2, x3, mask, (f & 1) ? 1.f : 0.f);
+}
+
+// 6x volume of the unit cube's part where G(u) = G0 + n.u > 0: the cube is
+// split into the 6 tets around its diagonal (0,0,0)-(1,1,1), each of 6x
+// volume 1, and each tet's inside fraction comes from the values of G at its
+// vertices -- non-negative terms only, so no cancellation, and the same
+// arithmetic for every lane.
+ADECO_HD inline float halfspace_cube_vol6(float G0, float nx, float ny, float nz)
+{
+    float G[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) G[k] = G0 + ((k & 1) ? nx : 0.f) + ((k & 2) ? ny : 0.f) + ((k & 4) ? nz : 0.f);
+    const int in0 = (int)(G[0] > 0.f), in7 = (int)(G[7] > 0.f);
+    const int path[6][2] = {{1, 3}, {1, 5}, {2, 3}, {2, 6}, {4, 5}, {4, 6}};
+    float v = 0.f;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+        const float x1 = G[path[q][0]], x2 = G[path[q][1]];
+        const int mask = in0 | ((int)(x1 > 0.f) << 1) | ((int)(x2 > 0.f) << 2) | (in7 << 3);
+        v += (mask == 15) ? 1.f : ((mask == 0) ? 0.f : side_fraction(G[0], x1, x2, G[7], mask, 0.f));
+    }
+    return v;
 }
 
 constexpr int kVolShift = 56;  // fixed point of 6x piece volumes (each <= 6)

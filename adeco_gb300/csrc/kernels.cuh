@@ -483,8 +483,13 @@ int classify_fp64(const WarpTets &W, const GridDesc &g, int s, int a, int b, int
     return all_in ? P_CELL_INSIDE : P_PARTIAL;
 }
 
-ADECO_HD inline int classify_pair(const WarpTets &W, const GridDesc &g, int s, int a, int b, int c, bool &used_fp64)
+// cross: the one tet face plane the cell straddles when the cell is certainly
+// inside the other three (then cell ∩ tet = cell ∩ that face's half-space),
+// else -1.
+ADECO_HD inline int classify_pair(const WarpTets &W, const GridDesc &g, int s, int a, int b, int c, bool &used_fp64,
+                                  int &cross)
 {
+    cross = -1;
     const float fa = (float)a, fb = (float)b, fc = (float)c;
     // strict AABB overlap with the cell [a,a+1] x [b,b+1] x [c,c+1]
     if (!(W.bmin[0][s] < fa + 1.f && fa < W.bmax[0][s] && W.bmin[1][s] < fb + 1.f && fb < W.bmax[1][s] &&
@@ -494,6 +499,7 @@ ADECO_HD inline int classify_pair(const WarpTets &W, const GridDesc &g, int s, i
         W.bmin[2][s] >= fc && W.bmax[2][s] <= fc + 1.f)
         return P_TET_INSIDE;
     bool all_in = true, unsure = false;
+    int ncross = 0, fcross = 0;
     const float t = W.tol[s];
 #pragma unroll
     for (int f = 0; f < 4; ++f) {
@@ -506,13 +512,44 @@ ADECO_HD inline int classify_pair(const WarpTets &W, const GridDesc &g, int s, i
         if (mx <= t) unsure = true;
         if (mn > t) continue;
         all_in = false;
+        ++ncross;
+        fcross = f;
         if (mn > -t) unsure = true;
     }
     if (unsure) {
         used_fp64 = true;
         return classify_fp64(W, g, s, a, b, c);
     }
+    if (ncross == 1) cross = fcross;
     return all_in ? P_CELL_INSIDE : P_PARTIAL;
+}
+
+// 6x volume of cell (a, b, c) ∩ slot s's tet when the cell straddles only
+// face f.  The face's linear function is taken about the face's centroid
+// (from the FP64 vertices q + qlo, in FP64), so that the FP32 rounding of
+// its normal only turns the plane about the centroid: the volume a slightly
+// turned plane adds on one side of the centroid it removes on the other,
+// and the tet's mass stays conserved over its cells.
+#ifdef __CUDA_ARCH__
+__device__ __noinline__
+#else
+inline
+#endif
+float halfspace_pair_vol6(const WarpTets &W, const GridDesc &g, int s, int a, int b, int c, int f)
+{
+    // faces (0,2,1) (0,3,2) (0,1,3) (1,2,3): the vertex a face leaves out
+    const int skip = (f == 0) ? 3 : ((f == 1) ? 1 : ((f == 2) ? 2 : 0));
+    const int cc[3] = {a, b, c};
+    double G0 = 0.0;
+#pragma unroll
+    for (int x = 0; x < 3; ++x) {
+        double sum = 0.0;
+#pragma unroll
+        for (int v = 0; v < 4; ++v)
+            if (v != skip) sum += (double)W.q[3 * v + x][s] + (double)W.qlo[3 * v + x][s];
+        G0 += (double)W.n[f][x][s] * ((double)cc[x] * g.rcell[x] - sum * (1.0 / 3.0));
+    }
+    return halfspace_cube_vol6((float)G0, W.n[f][0][s], W.n[f][1][s], W.n[f][2][s]);
 }
 
 // mass (FP64) of one (tet, cell) pair -> 64-bit fixed point, added to the cell
@@ -780,7 +817,8 @@ __global__ void __launch_bounds__(kThreads, 3) deposit_mixed_kernel(DepositParam
                         const int a = local % ex0, r = local / ex0, b = r % ex1, c = r / ex1;
                         ++st_cand;
                         bool f64 = false;
-                        const int cls = classify_pair(W, g, s, a, b, c, f64);
+                        int cross = -1;
+                        const int cls = classify_pair(W, g, s, a, b, c, f64, cross);
                         st_fp64 += f64;
                         if (cls == P_TET_INSIDE) {
                             ++st_in;
@@ -793,8 +831,13 @@ __global__ void __launch_bounds__(kThreads, 3) deposit_mixed_kernel(DepositParam
                         } else if (cls == P_PARTIAL) {
                             ++st_part;
                             ++st_bbox;
-                            part = true;
-                            entry = ((uint32_t)s << 27) | (uint32_t)local;
+                            if (cross >= 0) {  // one face cuts the cell: closed form, no clipping
+                                const double dm = (double)halfspace_pair_vol6(W, g, s, a, b, c, cross) * W.factor6[s];
+                                if (dm > 0.0) scatter(P, g, W, s, a, b, c, dm);
+                            } else {
+                                part = true;
+                                entry = ((uint32_t)s << 27) | (uint32_t)local;
+                            }
                         }
                     }
                     const unsigned bal = __ballot_sync(0xffffffffu, part);
