@@ -786,14 +786,19 @@ __global__ void __launch_bounds__(kThreads, 3) deposit_mixed_kernel(DepositParam
                     if (lane >= o) sincl += y;
                 }
                 const int sbase = sincl - len0 - len1;
-                W.seg_scan[2 * lane] = sbase;
-                W.seg_scan[2 * lane + 1] = sbase + len0;
-                W.seg_start[2 * lane] = st0;
-                W.seg_start[2 * lane + 1] = st1;
-                W.seg_s[2 * lane] = (uint8_t)sslot;
-                W.seg_s[2 * lane + 1] = (uint8_t)sslot;
                 const int total = __shfl_sync(0xffffffffu, sincl, 31);
-                if (lane == 31) W.seg_scan[64] = total;
+                if (rb < 0) {  // one segment per slot: slot = segment, start 0
+                    W.seg_scan[lane] = sbase;
+                    if (lane == 31) W.seg_scan[32] = total;
+                } else {
+                    W.seg_scan[2 * lane] = sbase;
+                    W.seg_scan[2 * lane + 1] = sbase + len0;
+                    W.seg_start[2 * lane] = st0;
+                    W.seg_start[2 * lane + 1] = st1;
+                    W.seg_s[2 * lane] = (uint8_t)sslot;
+                    W.seg_s[2 * lane + 1] = (uint8_t)sslot;
+                    if (lane == 31) W.seg_scan[64] = total;
+                }
                 __syncwarp();
                 const bool last_pass = rb + 32 >= total_rows;
                 for (int pb = 0;; pb += 32) {
@@ -807,12 +812,20 @@ __global__ void __launch_bounds__(kThreads, 3) deposit_mixed_kernel(DepositParam
                     bool part = false;
                     uint32_t entry = 0;
                     if (pidx < total) {
-                        int sg = 0;
+                        int sg = 0, s, local;
+                        if (rb < 0) {
 #pragma unroll
-                        for (int step = 32; step > 0; step >>= 1)
-                            if (W.seg_scan[sg + step] <= pidx) sg += step;
-                        const int s = W.seg_s[sg];
-                        const int local = W.seg_start[sg] + (pidx - W.seg_scan[sg]);
+                            for (int step = 16; step > 0; step >>= 1)
+                                if (W.seg_scan[sg + step] <= pidx) sg += step;
+                            s = sg;
+                            local = pidx - W.seg_scan[sg];
+                        } else {
+#pragma unroll
+                            for (int step = 32; step > 0; step >>= 1)
+                                if (W.seg_scan[sg + step] <= pidx) sg += step;
+                            s = W.seg_s[sg];
+                            local = W.seg_start[sg] + (pidx - W.seg_scan[sg]);
+                        }
                         const int ex0 = W.ex[0][s], ex1 = W.ex[1][s];
                         const int a = local % ex0, r = local / ex0, b = r % ex1, c = r / ex1;
                         ++st_cand;
