@@ -76,10 +76,7 @@ struct WarpTets {
     double factor6[32];  // mass per unit of 6x clipped volume (FP64)
     int lo[3][32];       // anchor cell (first candidate cell) in grid indices
     int ex[3][32];       // candidate extents (cells per axis)
-    int scan[33];        // exclusive prefix of candidate counts (row counts while walking rows)
-    int seg_scan[65];    // row walk: exclusive prefix of the segment lengths
-    int seg_start[64];   // row walk: first local pair index of each segment
-    uint8_t seg_s[64];   // row walk: slot of each segment
+    int scan[33];        // exclusive prefix of candidate counts
     int tetid[32];       // staged cube * 6 + tet of the slot (FP64 route)
 };
 
@@ -605,184 +602,6 @@ __device__ __forceinline__ void clip_list(const DepositParams &P, const GridDesc
     __syncwarp();
 }
 
-// ---------------------------------------------------------- row walking
-// Tets with at least kRowMinPairs candidate cells and kRowMinCells cells
-// along x (cells much smaller than the tet: zoom boxes at fine resolution)
-// are walked row by row in a routine of their own, so that the common case
-// -- a few cells per tet -- runs none of its code.
-constexpr int kRowMinPairs = 64;
-constexpr int kRowMinCells = 4;
-
-struct PairCounts {
-    unsigned cand, bbox, in, cin, part, fp64, fb;
-};
-
-// Cells of row (b, c) of slot s's candidate box: [lo_c, hi_c] may meet the
-// tet, [lo_i, hi_i] are certainly inside it (empty when lo > hi).  Along the
-// row the plane bounds of classify_pair are linear in the cell index a, so
-// each plane gives a bound on a; the candidate range is widened and the
-// inside range narrowed by a cell so that FP32 rounding of the bounds cannot
-// misplace a cell: cells outside [lo_c, hi_c] cannot meet the tet, cells in
-// [lo_i, hi_i] are CELL_INSIDE_TET, and the rest go through classify_pair.
-ADECO_HD inline void row_intervals(const WarpTets &W, int s, int b, int c, int &lo_c, int &hi_c, int &lo_i,
-                                   int &hi_i)
-{
-    const float top = (float)(W.ex[0][s] - 1);
-    const float fb = (float)b, fc = (float)c, t = W.tol[s];
-    float c0 = 0.f, c1 = top, i0 = 0.f, i1 = top;
-    bool none = false, no_in = false;
-#pragma unroll
-    for (int f = 0; f < 4; ++f) {
-        const float nx = W.n[f][0][s], ny = W.n[f][1][s], nz = W.n[f][2][s];
-        const float base = fmaf(ny, fb, fmaf(nz, fc, -W.d[f][s]));
-        const float pos = fmaxf(nx, 0.f) + fmaxf(ny, 0.f) + fmaxf(nz, 0.f);
-        const float kc = base + pos;                     // max over the cell: nx a + kc
-        const float ki = base + ((nx + ny + nz) - pos);  // min over the cell: nx a + ki
-        if (nx > 0.f) {
-            c0 = fmaxf(c0, floorf((-t - kc) / nx));
-            i0 = fmaxf(i0, floorf((t - ki) / nx) + 2.f);
-        } else if (nx < 0.f) {
-            c1 = fminf(c1, ceilf((-t - kc) / nx));
-            i1 = fminf(i1, ceilf((t - ki) / nx) - 2.f);
-        } else {
-            none = none || kc < -t;
-            no_in = no_in || !(ki > t);
-        }
-    }
-    c0 = fmaxf(c0, 0.f);
-    c1 = fminf(c1, top);
-    i0 = fmaxf(i0, c0);
-    i1 = fminf(i1, c1);
-    lo_c = (int)c0;
-    hi_c = none ? lo_c - 1 : (int)c1;
-    lo_i = (int)i0;
-    hi_i = (none || no_in) ? lo_i - 1 : (int)i1;
-}
-
-#ifdef __CUDACC__
-// Big tets of the warp's group (lanes in `big`): 32 rows at a time, the
-// inside cells of each row filled directly, the row ends classified, cut by
-// one face in closed form, the rest clipped.  Whole warp.
-__device__ __noinline__ void walk_big_tets(const DepositParams &P, const GridDesc &g, WarpTets &W, WarpPool &pool,
-                                           uint32_t *Q, bool big, PairCounts &k)
-{
-    const int lane = threadIdx.x & 31;
-    const int rows = big ? W.ex[1][lane] * W.ex[2][lane] : 0;
-    int rincl = rows;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(0xffffffffu, rincl, o);
-        if (lane >= o) rincl += y;
-    }
-    __syncwarp();
-    W.scan[lane] = rincl - rows;
-    const int total_rows = __shfl_sync(0xffffffffu, rincl, 31);
-    if (lane == 31) W.scan[32] = total_rows;
-    __syncwarp();
-    int np = 0;
-    for (int rb = 0; rb < total_rows; rb += 32) {
-        int len0 = 0, len1 = 0, st0 = 0, st1 = 0, sslot = 0;
-        if (rb + lane < total_rows) {
-            const int ridx = rb + lane;
-            int t = 0;
-#pragma unroll
-            for (int step = 16; step > 0; step >>= 1)
-                if (W.scan[t + step] <= ridx) t += step;
-            sslot = t;
-            const int rl = ridx - W.scan[t];
-            const int ex0 = W.ex[0][t], ex1 = W.ex[1][t];
-            const int b = rl % ex1, c = rl / ex1;
-            int lo_c, hi_c, lo_i, hi_i;
-            row_intervals(W, t, b, c, lo_c, hi_c, lo_i, hi_i);
-            if (lo_i <= hi_i) {
-                const unsigned n_in = hi_i - lo_i + 1;
-                k.cin += n_in;
-                k.cand += n_in;
-                k.bbox += n_in;
-                const unsigned long long fx = (unsigned long long)llrint(ldexp(6.0 * W.factor6[t], g.shift));
-                const long long j = W.lo[1][t] + b, kk = W.lo[2][t] + c;
-                unsigned long long *row =
-                    P.out + g.out_offset + W.lo[0][t] + (long long)g.dims * (j + (long long)g.dims * kk);
-                if (fx)
-                    for (int a = lo_i; a <= hi_i; ++a) atomicAdd(row + a, fx);
-                st0 = rl * ex0 + lo_c;
-                len0 = lo_i - lo_c;
-                st1 = rl * ex0 + hi_i + 1;
-                len1 = hi_c - hi_i;
-            } else if (lo_c <= hi_c) {
-                st0 = rl * ex0 + lo_c;
-                len0 = hi_c - lo_c + 1;
-            }
-        }
-        int sincl = len0 + len1;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int y = __shfl_up_sync(0xffffffffu, sincl, o);
-            if (lane >= o) sincl += y;
-        }
-        const int sbase = sincl - len0 - len1;
-        const int total = __shfl_sync(0xffffffffu, sincl, 31);
-        W.seg_scan[2 * lane] = sbase;
-        W.seg_scan[2 * lane + 1] = sbase + len0;
-        W.seg_start[2 * lane] = st0;
-        W.seg_start[2 * lane + 1] = st1;
-        W.seg_s[2 * lane] = (uint8_t)sslot;
-        W.seg_s[2 * lane + 1] = (uint8_t)sslot;
-        if (lane == 31) W.seg_scan[64] = total;
-        __syncwarp();
-        const bool last_pass = rb + 32 >= total_rows;
-        for (int pb = 0;; pb += 32) {
-            if (np > kQueue - 32 || (pb >= total && np && last_pass)) {
-                clip_list(P, g, W, pool, Q, np, k.fb);
-                np = 0;
-            }
-            if (pb >= total) break;
-            const int pidx = pb + lane;
-            bool part = false;
-            uint32_t entry = 0;
-            if (pidx < total) {
-                int sg = 0;
-#pragma unroll
-                for (int step = 32; step > 0; step >>= 1)
-                    if (W.seg_scan[sg + step] <= pidx) sg += step;
-                const int s = W.seg_s[sg];
-                const int local = W.seg_start[sg] + (pidx - W.seg_scan[sg]);
-                const int ex0 = W.ex[0][s], ex1 = W.ex[1][s];
-                const int a = local % ex0, r = local / ex0, b = r % ex1, c = r / ex1;
-                ++k.cand;
-                bool f64 = false;
-                int cross = -1;
-                const int cls = classify_pair(W, g, s, a, b, c, f64, cross);
-                k.fp64 += f64;
-                if (cls == P_TET_INSIDE) {
-                    ++k.in;
-                    ++k.bbox;
-                    scatter(P, g, W, s, a, b, c, (double)g.tet_mass);
-                } else if (cls == P_CELL_INSIDE) {
-                    ++k.cin;
-                    ++k.bbox;
-                    scatter(P, g, W, s, a, b, c, 6.0 * W.factor6[s]);
-                } else if (cls == P_PARTIAL) {
-                    ++k.part;
-                    ++k.bbox;
-                    if (cross >= 0) {
-                        const double dm = (double)halfspace_pair_vol6(W, g, s, a, b, c, cross) * W.factor6[s];
-                        if (dm > 0.0) scatter(P, g, W, s, a, b, c, dm);
-                    } else {
-                        part = true;
-                        entry = ((uint32_t)s << 27) | (uint32_t)local;
-                    }
-                }
-            }
-            const unsigned bal = __ballot_sync(0xffffffffu, part);
-            if (part) Q[np + __popc(bal & ((1u << lane) - 1))] = entry;
-            np += __popc(bal);
-            __syncwarp();
-        }
-    }
-}
-#endif
-
 // -------------------------------------------------- mixed batched kernel
 // Persistent: CTAs take work items (grid x vertex block) from a global
 // counter; inside an item the warps take groups of 32 tets from a shared
@@ -848,17 +667,14 @@ __global__ void __launch_bounds__(kThreads, 3) deposit_mixed_kernel(DepositParam
             route64 = route64 && cnt > 0;
             if (route64) cnt = 0;  // deposited below by the FP64 route
             unsigned fp64_tets = __ballot_sync(0xffffffffu, route64);
-            // tets spanning many cells are walked row by row afterwards
-            const bool big = cnt >= kRowMinPairs && W.ex[0][lane] >= kRowMinCells;
-            const int pcnt = big ? 0 : cnt;
             // exclusive scan of the pair counts across the warp
-            int incl = pcnt;
+            int incl = cnt;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
                 const int y = __shfl_up_sync(0xffffffffu, incl, o);
                 if (lane >= o) incl += y;
             }
-            W.scan[lane] = incl - pcnt;
+            W.scan[lane] = incl - cnt;
             const int total = __shfl_sync(0xffffffffu, incl, 31);
             if (lane == 31) W.scan[32] = total;
             __syncwarp();
@@ -910,17 +726,6 @@ __global__ void __launch_bounds__(kThreads, 3) deposit_mixed_kernel(DepositParam
                 if (part) Q[np + __popc(bal & ((1u << lane) - 1))] = entry;
                 np += __popc(bal);
                 __syncwarp();
-            }
-            if (__any_sync(0xffffffffu, big)) {
-                PairCounts k = {st_cand, st_bbox, st_in, st_cin, st_part, st_fp64, st_fb};
-                walk_big_tets(P, g, W, pool, Q, big, k);
-                st_cand = k.cand;
-                st_bbox = k.bbox;
-                st_in = k.in;
-                st_cin = k.cin;
-                st_part = k.part;
-                st_fp64 = k.fp64;
-                st_fb = k.fb;
             }
             // ill-conditioned tets of this group: whole warp, FP64
             while (fp64_tets) {
