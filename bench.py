@@ -506,6 +506,8 @@ def run_serve(args, rank, ws, local):
         i = 0
         while i < len(stream) or pending:
             now = time.perf_counter() - t_start
+            if now > args.serve_seconds + args.serve_drain_s:
+                break  # overloaded: stop waiting, report what finished and what did not
             while i < len(stream) and stream[i][0] <= now:
                 try:
                     pending[s.submit([stream[i][1]])] = stream[i][0]
@@ -521,6 +523,10 @@ def run_serve(args, rank, ws, local):
                     s.release(b)
             time.sleep(0.0002)
         wall = time.perf_counter() - t_start
+        unfinished = len(pending) + (len(stream) - i)
+        for b in list(pending):
+            s.wait(b)
+            s.release(b)
     lat = np.sort(np.asarray(lat))
     line = {
         "metric": "serving latency p50", "value": float(np.percentile(lat, 50)), "unit": "ms", "n_gpus": 1,
@@ -532,7 +538,7 @@ def run_serve(args, rank, ws, local):
         "p50_ms": float(np.percentile(lat, 50)), "p90_ms": float(np.percentile(lat, 90)),
         "p99_ms": float(np.percentile(lat, 99)), "max_ms": float(lat[-1]),
         "requests": len(lat), "offered_rate": args.serve_rate, "achieved_rate": len(lat) / wall,
-        "admission_retries": refused,
+        "admission_retries": refused, "unfinished_at_deadline": unfinished,
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -558,6 +564,7 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--serve-dims", type=int, nargs="+", default=[32, 64, 128, 256, 512])
+    ap.add_argument("--serve-drain-s", type=float, default=30.0)
     args = ap.parse_args()
     set_workload(args.workload)
     if args.n:
