@@ -393,7 +393,18 @@ __device__ __noinline__ void deposit_tet_fp64_warp(const float3 v[4], const int 
                 p[q][2] = qd[q][2] - ok;
             }
             ++n_part;
-            dm = clip_volume6<double, double>(p) * f6;
+            if (kFixed) {
+                // mixed path: FP32 clipping in the tet's barycentric frame, the
+                // share of the tet times its exact mass
+                float X[4][3];
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+#pragma unroll
+                    for (int x = 0; x < 3; ++x) X[q][x] = (float)p[q][x];
+                dm = clip_bary_fraction(X) * g.mass_factor;
+            } else {
+                dm = clip_volume6<double, double>(p) * f6;
+            }
         }
         if (!(dm > 0.0)) return;
         put(g.out_offset + (lo[0] + a) + (long long)g.dims * ((lo[1] + b) + (long long)g.dims * (lo[2] + k)), dm);
