@@ -447,7 +447,7 @@ def run_zoom(args, rank, ws, local):
     if rank != 0:
         return 0
     pos = workload_positions()
-    reqs = zoom_requests(ZOOM_COUNT, L=L_BOX, seed=ZOOM_SEED, dims=tuple(args.zoom_dims))
+    reqs = zoom_requests(args.zoom_count, L=L_BOX, seed=ZOOM_SEED, dims=tuple(args.zoom_dims))
     cells = sum(r[2] ** 3 for r in reqs)
     dev, host = [], []
     same = None
@@ -561,6 +561,7 @@ def main():
     ap.add_argument("--n", type=int, default=None, help="lattice size; the benchmark workload is 256")
     ap.add_argument("--workload", default="c2", choices=["c2", "c4", "zoom", "serve"])
     ap.add_argument("--zoom-dims", type=int, nargs="+", default=[32, 64, 128, 256])
+    ap.add_argument("--zoom-count", type=int, default=ZOOM_COUNT)
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--serve-dims", type=int, nargs="+", default=[32, 64, 128, 256, 512])
