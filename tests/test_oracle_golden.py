@@ -97,3 +97,20 @@ def test_empty_input_is_a_no_op(oracle):
     oracle.deposit_patches(np.zeros(0, np.float32), 7, np.array([0, 1, 0, 1, 0, 1], np.float32), 2,
                            fp64=False, grid=grid, num_patches=0)
     assert np.all(grid == 1)
+
+
+def test_reader_restatement_matches_reference_fixtures(tmp_path):
+    """oracle/readers.py against the lattices the reference's own readers made
+    from the same SORTED_BY_ID / DARK_SKY files (bit-exact, bbox included)."""
+    import sys
+    from oracle import readers as R
+    sys.path.insert(0, str(GOLDEN))
+    from make_golden_readers import CASES, write_inputs
+    g = load_golden("readers.npz")
+    paths = write_inputs(g["lattice"], str(tmp_path))
+    for k, (fmt, stride, periodic) in enumerate(CASES):
+        xyz, bbox = R.read_particles(paths[fmt], fmt, stride, bool(periodic))
+        assert np.array_equal(xyz, g[f"xyz_{k}"]), (fmt, stride, periodic)
+        assert np.array_equal(bbox, g[f"bbox_{k}"])
+    with pytest.raises(ValueError):
+        R.read_particles(paths["DARK_SKY"], "DARK_SKY", 3, True)   # 16 is not a multiple of 3
