@@ -17,9 +17,10 @@ HEADER = os.path.join(ROOT, "include", "adeco_deposit.h")
 OK = 0
 STATUS_NAMES = {0: "OK", 1: "ERR_ARGUMENT", 2: "ERR_OVERFLOW", 3: "ERR_DEVICE", 4: "ERR_CUDA", 5: "ERR_MEMORY",
                 6: "ERR_INCONSISTENT", 7: "ERR_STATE", 8: "ERR_NOT_FOUND", 9: "ERR_LIMIT"}
-ERR_MEMORY = 5
+ERR_ARGUMENT, ERR_MEMORY = 1, 5
 PREC_MIXED, PREC_FP64 = 0, 1
 ORDER_REF, ORDER_CONFORMING = 0, 1
+FORMAT_SORTED_BY_ID, FORMAT_DARK_SKY = 0, 1
 OUT_F32, OUT_F64 = 0, 1
 
 
@@ -77,6 +78,9 @@ _SIGS = {
     "adeco_deposit_tets_device_noalloc": ([_vp, _sz, _sz, _sz, _i, _vp, _i, _vp, _i, _d, _vp], _i),
     "adeco_session_create": ([C.POINTER(SessionConfig), _vp, _i, _i, _i, C.POINTER(_vp)], _i),
     "adeco_session_destroy": ([_vp], _i),
+    "adeco_session_create_from_file": ([C.POINTER(SessionConfig), C.c_char_p, _i, _i, _i, _vp, C.POINTER(_vp)], _i),
+    "adeco_session_lattice_dims": ([_vp, _vp], _i),
+    "adeco_session_positions": ([_vp, _vp, _sz], _i),
     "adeco_session_bbox": ([_vp, _vp], _i),
     "adeco_session_build_octree": ([_vp, _vp, _vp, C.c_uint64, _i, _i], _i),
     "adeco_session_octree_size": ([_vp, C.POINTER(_i), C.POINTER(_i), C.POINTER(_i)], _i),

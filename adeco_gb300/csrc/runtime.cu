@@ -500,6 +500,206 @@ __global__ void xyz_to_float4_kernel(const float *xyz, float4 *out, long long n)
         out[i] = make_float4(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], 0.f);
 }
 
+// Device, stream and kernel set-up of a new session (the lattice is filled by the caller).
+static int session_open(const adeco_session_config *cfg, adeco_session &S)
+{
+    if (cfg) {
+        S.device = cfg->device;
+        S.order = cfg->tet_order;
+        S.tet_mass = cfg->tet_mass > 0 ? cfg->tet_mass : 1.0;
+        S.hbm_fraction = cfg->hbm_fraction > 0 ? cfg->hbm_fraction : 0.75;
+        S.acc_fp64 = cfg->accumulate_fp64;
+    }
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0) return fail(ADECO_ERR_DEVICE, "no CUDA device");
+    if (S.device < 0 || S.device >= count) return fail(ADECO_ERR_DEVICE, "invalid device %d", S.device);
+    CUDA_TRY(cudaSetDevice(S.device));
+    int rc = mixed_setup(S.device, S.dp);
+    if (rc) return rc;
+    CUDA_TRY(cudaStreamCreateWithFlags(&S.stream, cudaStreamNonBlocking));
+    return ADECO_OK;
+}
+
+// Meta-cell AABBs of the resident lattice (MetaMesh), on the device; their
+// union into bbox6 (xmin,xmax,...) when bbox6 is non-null.
+static int session_meta_bbox(adeco_session &S, float *bbox6)
+{
+    S.meta.init(S.nx, S.ny, S.nz);
+    const long long nmc = (long long)S.meta.count();
+    DevBuf<float> d_bb;
+    int rc;
+    if ((rc = d_bb.reserve((size_t)nmc * 6))) return rc;
+    meta_bbox_kernel<<<(unsigned)((nmc * 32 + 255) / 256), 256, 0, S.stream>>>(S.lattice.p, S.nx, S.ny, S.nz, S.meta.cd[0],
+                                                                                  S.meta.cd[1], S.meta.cd[2], d_bb.p);
+    CUDA_TRY(cudaGetLastError());
+    S.meta.bbox.resize((size_t)nmc * 6);
+    CUDA_TRY(cudaMemcpyAsync(S.meta.bbox.data(), d_bb.p, (size_t)nmc * 6 * sizeof(float), cudaMemcpyDeviceToHost,
+                             S.stream));
+    CUDA_TRY(cudaStreamSynchronize(S.stream));
+    if (bbox6) {
+        float mn[3] = {3.4e38f, 3.4e38f, 3.4e38f}, mx[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+        for (size_t i = 0; i < S.meta.count(); ++i)
+            for (int a = 0; a < 3; ++a) {
+                mn[a] = std::min(mn[a], S.meta.bbox[6 * i + a]);
+                mx[a] = std::max(mx[a], S.meta.bbox[6 * i + 3 + a]);
+            }
+        for (int a = 0; a < 3; ++a) {
+            bbox6[2 * a] = mn[a];
+            bbox6[2 * a + 1] = mx[a];
+        }
+    }
+    return ADECO_OK;
+}
+
+// Meta-cells, bounding box and work counters once the lattice is resident.
+static int session_finish(adeco_session &S)
+{
+    int rc = session_meta_bbox(S, S.bbox6);
+    if (rc) return rc;
+    if ((rc = S.d_counter.reserve(2)) || (rc = S.d_stats.reserve(kNumStats))) return rc;
+    CUDA_TRY(cudaMemset(S.d_counter.p, 0, 2 * sizeof(int)));
+    return ADECO_OK;
+}
+
+#include "readers.cuh"
+
+// Reads `path` into the session's lattice (see readers.cuh).
+static int read_particle_file(adeco_session &S, const char *path, int format, int stride, int periodic, float bbox_out[6])
+{
+    HostFile hf;
+    hf.f = std::fopen(path, "rb");
+    if (!hf.f) return fail(ADECO_ERR_ARGUMENT, "failed to open file: %s", path);
+    std::fseek(hf.f, 0, SEEK_END);
+    const long long fsize = (long long)std::ftell(hf.f);
+    size_t first = 0, recsize = 12;
+    long long count = 0;
+    int n = 0, n0 = 0;
+    if (format == ADECO_FORMAT_SORTED_BY_ID) {
+        if (fsize % 12) return fail(ADECO_ERR_ARGUMENT, "inconsistent file size");
+        count = fsize / 12;
+        n0 = (int)std::llrint(std::cbrt((double)count));
+        if ((long long)n0 * n0 * n0 != count) return fail(ADECO_ERR_ARGUMENT, "lagrangian grid not cubical");
+        n = n0;  // the reference ignores the stride for this format
+    } else if (format == ADECO_FORMAT_DARK_SKY) {
+        int rc = sdf_header_size(hf.f, first);
+        if (rc) return rc;
+        recsize = 32;
+        if ((long long)first > fsize || (fsize - (long long)first) % 32)
+            return fail(ADECO_ERR_ARGUMENT, "inconsistent file size");
+        count = (fsize - (long long)first) / 32;
+        n0 = (int)std::llrint(std::cbrt((double)count));
+        if ((long long)n0 * n0 * n0 != count) return fail(ADECO_ERR_ARGUMENT, "lagrangian grid not cubical");
+        if (stride < 1 || n0 % stride) return fail(ADECO_ERR_ARGUMENT, "invalid stride %d for data dimensions %d", stride, n0);
+        n = n0 / stride;
+    } else {
+        return fail(ADECO_ERR_ARGUMENT, "unknown particle file format %d", format);
+    }
+    if (n < 2) return fail(ADECO_ERR_ARGUMENT, "lattice must be at least 2^3 (got %d^3)", n);
+    S.nx = S.ny = S.nz = n;
+    const long long total = (long long)n * n * n;
+    int rc;
+    if ((rc = S.lattice.reserve((size_t)total))) return rc;
+    DevBuf<unsigned long long> d_kept;
+    DevBuf<int> d_err;
+    if ((rc = d_kept.reserve(1)) || (rc = d_err.reserve(1))) return rc;
+    CUDA_TRY(cudaMemsetAsync(d_kept.p, 0, sizeof(unsigned long long), S.stream));
+    CUDA_TRY(cudaMemsetAsync(d_err.p, 0, sizeof(int), S.stream));
+    ChunkPipe pipe;
+    if ((rc = pipe.open())) return rc;
+    const long long per_chunk = (long long)(kReadChunk / recsize);
+    std::fseek(hf.f, (long)first, SEEK_SET);
+    long long done = 0;
+    for (int b = 0; done < count; b ^= 1) {
+        const long long nrec = std::min(per_chunk, count - done);
+        CUDA_TRY(cudaEventSynchronize(pipe.done[b]));  // this buffer's previous chunk is decoded
+        if (std::fread(pipe.host[b], recsize, (size_t)nrec, hf.f) != (size_t)nrec)
+            return fail(ADECO_ERR_ARGUMENT, "short read of %s", path);
+        CUDA_TRY(cudaMemcpyAsync(pipe.dev[b], pipe.host[b], (size_t)nrec * recsize, cudaMemcpyHostToDevice, S.stream));
+        const unsigned blocks = (unsigned)std::min<long long>((nrec + 255) / 256, 4096);
+        if (format == ADECO_FORMAT_SORTED_BY_ID)
+            sorted_chunk_kernel<<<blocks, 256, 0, S.stream>>>(reinterpret_cast<const float *>(pipe.dev[b]), done, nrec,
+                                                              S.lattice.p);
+        else
+            darksky_chunk_kernel<<<blocks, 256, 0, S.stream>>>(pipe.dev[b], nrec, n0, stride, n, S.lattice.p, d_kept.p,
+                                                               d_err.p);
+        CUDA_TRY(cudaGetLastError());
+        CUDA_TRY(cudaEventRecord(pipe.done[b], S.stream));
+        done += nrec;
+    }
+    CUDA_TRY(cudaStreamSynchronize(S.stream));
+    if (format == ADECO_FORMAT_DARK_SKY) {
+        unsigned long long kept = 0;
+        int err = 0;
+        CUDA_TRY(cudaMemcpy(&kept, d_kept.p, sizeof kept, cudaMemcpyDeviceToHost));
+        CUDA_TRY(cudaMemcpy(&err, d_err.p, sizeof err, cudaMemcpyDeviceToHost));
+        if (err) return fail(ADECO_ERR_ARGUMENT, "a particle id lies outside the %d^3 lattice", n0);
+        if ((long long)kept != total)
+            return fail(ADECO_ERR_ARGUMENT, "inconsistent global particle number (%llu of %lld)", kept, total);
+    }
+    // global bbox of the particles as read (the reference's global_bbox)
+    float bb[6];
+    if ((rc = session_meta_bbox(S, bb))) return rc;
+    if (bbox_out)
+        for (int k = 0; k < 6; ++k) bbox_out[k] = bb[k];
+    if (periodic) {
+        float e[3], lo[3], hi[3];
+        for (int a = 0; a < 3; ++a) {
+            const volatile float ext = bb[2 * a + 1] - bb[2 * a];  // FP32 steps, as the reference writes them
+            const volatile float q = ext / 4.0f;
+            const volatile float t = 0.75f * ext;
+            e[a] = ext;
+            lo[a] = bb[2 * a] + q;
+            hi[a] = bb[2 * a] + t;
+        }
+        const float half = (float)n / 2.0f;
+        unwrap_kernel<<<(unsigned)std::min<long long>((total + 255) / 256, 65535), 256, 0, S.stream>>>(
+            S.lattice.p, n, half, make_float3(e[0], e[1], e[2]), make_float3(lo[0], lo[1], lo[2]),
+            make_float3(hi[0], hi[1], hi[2]));
+        CUDA_TRY(cudaGetLastError());
+        CUDA_TRY(cudaStreamSynchronize(S.stream));
+    }
+    return ADECO_OK;
+}
+
+extern "C" int adeco_session_create_from_file(const adeco_session_config *cfg, const char *path, int format, int stride,
+                                              int periodic, float bbox_out[6], adeco_session **out)
+{
+    if (!out || !path) return fail(ADECO_ERR_ARGUMENT, "null path or output pointer");
+    *out = nullptr;
+    std::unique_ptr<adeco_session> s(new adeco_session());
+    int rc = session_open(cfg, *s);
+    if (rc) return rc;
+    if ((rc = read_particle_file(*s, path, format, stride, periodic, bbox_out))) return rc;
+    if ((rc = session_finish(*s))) return rc;
+    *out = s.release();
+    return ADECO_OK;
+}
+
+extern "C" int adeco_session_positions(adeco_session *s, float *xyz, size_t capacity)
+{
+    if (!s || !xyz) return fail(ADECO_ERR_ARGUMENT, "null argument");
+    const size_t n = (size_t)s->nx * s->ny * s->nz;
+    if (capacity < 3 * n) return fail(ADECO_ERR_ARGUMENT, "capacity %zu < %zu floats", capacity, 3 * n);
+    CUDA_TRY(cudaSetDevice(s->device));
+    std::vector<float4> tmp(n);
+    CUDA_TRY(cudaMemcpy(tmp.data(), s->lattice.p, n * sizeof(float4), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < n; ++i) {
+        xyz[3 * i] = tmp[i].x;
+        xyz[3 * i + 1] = tmp[i].y;
+        xyz[3 * i + 2] = tmp[i].z;
+    }
+    return ADECO_OK;
+}
+
+extern "C" int adeco_session_lattice_dims(adeco_session *s, int dims[3])
+{
+    if (!s || !dims) return fail(ADECO_ERR_ARGUMENT, "null argument");
+    dims[0] = s->nx;
+    dims[1] = s->ny;
+    dims[2] = s->nz;
+    return ADECO_OK;
+}
+
 extern "C" int adeco_session_create(const adeco_session_config *cfg, const float *positions, int nx, int ny, int nz,
                                     adeco_session **out)
 {
@@ -507,20 +707,8 @@ extern "C" int adeco_session_create(const adeco_session_config *cfg, const float
     *out = nullptr;
     if (nx < 2 || ny < 2 || nz < 2) return fail(ADECO_ERR_ARGUMENT, "lattice must be at least 2^3 (got %d,%d,%d)", nx, ny, nz);
     std::unique_ptr<adeco_session> s(new adeco_session());
-    if (cfg) {
-        s->device = cfg->device;
-        s->order = cfg->tet_order;
-        s->tet_mass = cfg->tet_mass > 0 ? cfg->tet_mass : 1.0;
-        s->hbm_fraction = cfg->hbm_fraction > 0 ? cfg->hbm_fraction : 0.75;
-        s->acc_fp64 = cfg->accumulate_fp64;
-    }
-    int count = 0;
-    if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0) return fail(ADECO_ERR_DEVICE, "no CUDA device");
-    if (s->device < 0 || s->device >= count) return fail(ADECO_ERR_DEVICE, "invalid device %d", s->device);
-    CUDA_TRY(cudaSetDevice(s->device));
-    int rc = mixed_setup(s->device, s->dp);
+    int rc = session_open(cfg, *s);
     if (rc) return rc;
-    CUDA_TRY(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
     s->nx = nx; s->ny = ny; s->nz = nz;
     const long long n = (long long)nx * ny * nz;
     if ((rc = s->lattice.reserve((size_t)n))) return rc;
@@ -530,30 +718,9 @@ extern "C" int adeco_session_create(const adeco_session_config *cfg, const float
         CUDA_TRY(cudaMemcpyAsync(raw.p, positions, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, s->stream));
         xyz_to_float4_kernel<<<std::min<long long>((n + 255) / 256, 65535), 256, 0, s->stream>>>(raw.p, s->lattice.p, n);
         CUDA_TRY(cudaGetLastError());
-        s->meta.init(nx, ny, nz);
-        const long long nmc = (long long)s->meta.count();
-        DevBuf<float> d_bb;
-        if ((rc = d_bb.reserve((size_t)nmc * 6))) return rc;
-        meta_bbox_kernel<<<(unsigned)((nmc * 32 + 255) / 256), 256, 0, s->stream>>>(
-            s->lattice.p, nx, ny, nz, s->meta.cd[0], s->meta.cd[1], s->meta.cd[2], d_bb.p);
-        CUDA_TRY(cudaGetLastError());
-        s->meta.bbox.resize((size_t)nmc * 6);
-        CUDA_TRY(cudaMemcpyAsync(s->meta.bbox.data(), d_bb.p, (size_t)nmc * 6 * sizeof(float), cudaMemcpyDeviceToHost,
-                                 s->stream));
         CUDA_TRY(cudaStreamSynchronize(s->stream));
     }
-    float mn[3] = {3.4e38f, 3.4e38f, 3.4e38f}, mx[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
-    for (size_t i = 0; i < s->meta.count(); ++i)
-        for (int a = 0; a < 3; ++a) {
-            mn[a] = std::min(mn[a], s->meta.bbox[6 * i + a]);
-            mx[a] = std::max(mx[a], s->meta.bbox[6 * i + 3 + a]);
-        }
-    for (int a = 0; a < 3; ++a) {
-        s->bbox6[2 * a] = mn[a];
-        s->bbox6[2 * a + 1] = mx[a];
-    }
-    if ((rc = s->d_counter.reserve(2)) || (rc = s->d_stats.reserve(kNumStats))) return rc;
-    CUDA_TRY(cudaMemset(s->d_counter.p, 0, 2 * sizeof(int)));
+    if ((rc = session_finish(*s))) return rc;
     *out = s.release();
     return ADECO_OK;
 }

@@ -136,6 +136,38 @@ class Session:
         self.leaf_dims = None
         self.tet_mass = tet_mass
 
+    @classmethod
+    def from_file(cls, path, fmt="DARK_SKY", *, stride=1, periodic=True, device=0, tet_order=L.ORDER_REF,
+                  tet_mass=1.0, hbm_fraction=0.75, accumulate_fp64=True):
+        """A session whose lattice is read from a SORTED_BY_ID or DARK_SKY particle
+        file (the reference's reader step); `read_bbox` holds the particles'
+        bounding box before the periodic unwrap."""
+        lib = L.load()
+        code = {"SORTED_BY_ID": L.FORMAT_SORTED_BY_ID, "DARK_SKY": L.FORMAT_DARK_SKY}
+        key = next((k for k in code if k in fmt), None)
+        if key is None:
+            raise AdRuntimeException(L.ERR_ARGUMENT, f"id_type {fmt} not supported")
+        cfg = L.SessionConfig(device, tet_order, tet_mass, hbm_fraction, int(bool(accumulate_fp64)))
+        bb = np.zeros(6, np.float32)
+        h = C.c_void_p()
+        _raise(lib.adeco_session_create_from_file(C.byref(cfg), os.fsencode(path), code[key], int(stride),
+                                                  int(bool(periodic)), _ptr(bb), C.byref(h)))
+        self = cls.__new__(cls)
+        self._h, self._lib = h, lib
+        dims = np.zeros(3, np.int32)
+        _raise(lib.adeco_session_lattice_dims(h, _ptr(dims)))
+        self.shape = (int(dims[2]), int(dims[1]), int(dims[0]))
+        self.leaf_dims = None
+        self.tet_mass = tet_mass
+        self.read_bbox = bb
+        return self
+
+    def positions(self):
+        """The resident lattice, (nz, ny, nx, 3) float32."""
+        out = np.zeros(self.shape + (3,), np.float32)
+        _raise(self._lib.adeco_session_positions(self._h, _ptr(out), out.size))
+        return out
+
     def close(self):
         if getattr(self, "_h", None):
             self._lib.adeco_session_destroy(self._h)

@@ -139,6 +139,25 @@ typedef struct {
 int adeco_session_create(const adeco_session_config *cfg, const float *positions, int nx, int ny, int nz,
                          adeco_session **out);
 int adeco_session_destroy(adeco_session *s);
+
+/* Particle file formats: the reference's id_type (src/AdPointDataReaders.h:914-930). */
+enum { ADECO_FORMAT_SORTED_BY_ID = 0, ADECO_FORMAT_DARK_SKY = 1 };
+/* A session whose lattice is read from a particle file, replacing the
+ * reference's reader step of deposit_workflow (src/AdDepositWorkFlow.h:74-111:
+ * AdPointDataReader::load_data on one rank, get_global_bbox_mpi,
+ * apply_boundary_corrections when periodic != 0).  SORTED_BY_ID: float32
+ * x,y,z per particle in id order (AdSortedByIdsPointDataReader, :770;
+ * stride ignored, as there).  DARK_SKY: SDF file of {x,y,z,vx,vy,vz float,
+ * int64 Morton id} records (AdDarkSkyDataReader, :361), every stride-th
+ * particle per axis kept.  bbox_out (may be null): the particles' bounding
+ * box before the unwrap -- the reference's global_bbox and default region of
+ * interest.  Errors (ADECO_ERR_ARGUMENT): unreadable file, bad header or
+ * size, non-cubic lattice, stride not dividing it, ids outside it. */
+int adeco_session_create_from_file(const adeco_session_config *cfg, const char *path, int format, int stride,
+                                   int periodic, float bbox_out[6], adeco_session **out);
+/* lattice size and the resident positions (3 floats per particle, x fastest) */
+int adeco_session_lattice_dims(adeco_session *s, int dims[3]);
+int adeco_session_positions(adeco_session *s, float *xyz, size_t capacity);
 /* particle AABB of the resident lattice: xmin,xmax,ymin,ymax,zmin,zmax */
 int adeco_session_bbox(adeco_session *s, float bbox[6]);
 
