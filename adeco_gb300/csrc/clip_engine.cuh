@@ -227,49 +227,52 @@ ADECO_HD inline float halfspace_cube_vol6(float G0, float nx, float ny, float nz
 // Fraction of a tet's volume inside the unit cube, for tets too flat for the
 // FP32 engine.  A flat tet's volume L^2 h, computed from FP32 coordinates as
 // a determinant, carries an error ~ 2^-24 L^3 -- relative 2^-24 kappa.  Here
-// the pieces are kept as barycentric coordinates of the tet (4 weights per
-// vertex): clipping is affine, so the cut parameters come from the cell-face
-// coordinates x = sum w_i X_i as before, but a piece's share of the tet is
+// every piece also carries its barycentric coordinates in the tet (4 weights
+// per vertex): clipping is affine, so a cut point's weights follow from the
+// same edge parameter t as its coordinates, and a piece's share of the tet is
 // the determinant of its weights -- well conditioned whatever the tet's
-// shape -- and the mass is that share times the tet's exact mass.  The
-// splits, the last-face fractions and the face order are the engine's.
+// shape; the mass is that share times the tet's exact mass.  Face tests, cut
+// points (snapped onto the face), splits, last-face fractions and the face
+// order are the engine's, on the piece's own coordinates.
 ADECO_HD inline double clip_bary_fraction(const float X[4][3])
 {
     constexpr int kDepth = 16;
-    float stk[kDepth][16];  // 4 vertices x 4 weights
+    constexpr int kRec = 28;  // 16 weights (4 per vertex) + 12 coordinates
+    float stk[kDepth][kRec];
     int sface[kDepth];
 #pragma unroll
     for (int i = 0; i < 16; ++i) stk[0][i] = (i % 5 == 0) ? 1.f : 0.f;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) stk[0][16 + 3 * j + a] = X[j][a];
     sface[0] = 0;
     int sp = 1;
     double acc = 0.0;
     while (sp > 0) {
         --sp;
-        float w[16];
+        float r[kRec];
 #pragma unroll
-        for (int i = 0; i < 16; ++i) w[i] = stk[sp][i];
+        for (int i = 0; i < kRec; ++i) r[i] = stk[sp][i];
+        const float *w = r, *x = r + 16;
         const int face0 = sface[sp];
-        // cell-frame coordinates of the piece's vertices
-        float x[4][3];
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-#pragma unroll
-            for (int a = 0; a < 3; ++a)
-                x[j][a] = fmaf(w[4 * j], X[0][a], fmaf(w[4 * j + 1], X[1][a], fmaf(w[4 * j + 2], X[2][a], w[4 * j + 3] * X[3][a])));
-        const int b0 = face_bits(x[0][0], x[0][1], x[0][2]), b1 = face_bits(x[1][0], x[1][1], x[1][2]);
-        const int b2 = face_bits(x[2][0], x[2][1], x[2][2]), b3 = face_bits(x[3][0], x[3][1], x[3][2]);
+        const int b0 = face_bits(x[0], x[1], x[2]), b1 = face_bits(x[3], x[4], x[5]);
+        const int b2 = face_bits(x[6], x[7], x[8]), b3 = face_bits(x[9], x[10], x[11]);
         const int all_in = b0 & b1 & b2 & b3, any_in = b0 | b1 | b2 | b3;
         const int relevant = (63 >> face0) << face0;
         if ((~any_in) & relevant) continue;  // beyond a face
-        // the piece's share of the tet: |det| of its weight differences (weights 1..3)
-        float d[3][3];
+        // the piece's share of the tet: the determinant of its weight
+        // differences (weights 1..3), signed -- every piece keeps the tet's
+        // orientation, and taking |det| would round near-degenerate pieces
+        // up and bias the sum
+        double d[3][3];
 #pragma unroll
         for (int j = 0; j < 3; ++j)
 #pragma unroll
-            for (int i = 0; i < 3; ++i) d[j][i] = w[4 * (j + 1) + i + 1] - w[i + 1];
-        const double share = fabs((double)d[0][0] * ((double)d[1][1] * d[2][2] - (double)d[1][2] * d[2][1]) -
-                                  (double)d[0][1] * ((double)d[1][0] * d[2][2] - (double)d[1][2] * d[2][0]) +
-                                  (double)d[0][2] * ((double)d[1][0] * d[2][1] - (double)d[1][1] * d[2][0]));
+            for (int i = 0; i < 3; ++i) d[j][i] = (double)w[4 * (j + 1) + i + 1] - (double)w[i + 1];
+        const double share = d[0][0] * (d[1][1] * d[2][2] - d[1][2] * d[2][1]) -
+                             d[0][1] * (d[1][0] * d[2][2] - d[1][2] * d[2][0]) +
+                             d[0][2] * (d[1][0] * d[2][1] - d[1][1] * d[2][0]);
         const int next = (~all_in) & relevant;
         if (!next) {
             acc += share;
@@ -283,7 +286,7 @@ ADECO_HD inline double clip_bary_fraction(const float X[4][3])
         const int axis = f >> 1;
         const float plane = (f & 1) ? 1.f : 0.f;
         const int mask = ((b0 >> f) & 1) | (((b1 >> f) & 1) << 1) | (((b2 >> f) & 1) << 2) | (((b3 >> f) & 1) << 3);
-        const float xa[4] = {x[0][axis], x[1][axis], x[2][axis], x[3][axis]};
+        const float xa[4] = {x[axis], x[3 + axis], x[6 + axis], x[9 + axis]};
         if ((next >> (f + 1)) == 0) {  // last crossed face: the inside fraction of the piece
             acc += share * (double)side_fraction(xa[0], xa[1], xa[2], xa[3], mask, plane);
             continue;
@@ -294,13 +297,16 @@ ADECO_HD inline double clip_bary_fraction(const float X[4][3])
         // edges: k=1: AB AC AD; k=2: AC AD BC BD; k=3: AD BD CD
         const int ein[4] = {0, (k == 3) ? 1 : 0, (k == 1) ? 0 : ((k == 2) ? 1 : 2), 1};
         const int eout[4] = {(k == 1) ? 1 : ((k == 2) ? 2 : 3), (k == 1) ? 2 : 3, (k == 2) ? 2 : 3, 3};
-        float E[4][4];
+        float E[4][7];  // cut points: 4 weights + 3 coordinates
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
             const int vi = id[ein[e]], vo = id[eout[e]];
             const float t = fminf(fmaxf((plane - xa[vi]) / (xa[vo] - xa[vi]), 0.f), 1.f);
 #pragma unroll
             for (int i = 0; i < 4; ++i) E[e][i] = fmaf(t, w[4 * vo + i] - w[4 * vi + i], w[4 * vi + i]);
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+                E[e][4 + a] = (a == axis) ? plane : fmaf(t, x[3 * vo + a] - x[3 * vi + a], x[3 * vi + a]);
         }
         // children as vertex lists: indices 0..3 = A..D (permuted), 4..7 = E0..E3
         const int ch[3][4] = {{0, k == 1 ? 4 : 1, k == 1 ? 5 : (k == 2 ? 6 : 2), k == 1 ? 6 : (k == 2 ? 7 : 6)},
@@ -313,6 +319,8 @@ ADECO_HD inline double clip_bary_fraction(const float X[4][3])
                 const int src = ch[c][v];
 #pragma unroll
                 for (int i = 0; i < 4; ++i) stk[sp][4 * v + i] = (src < 4) ? w[4 * id[src] + i] : E[src - 4][i];
+#pragma unroll
+                for (int a = 0; a < 3; ++a) stk[sp][16 + 3 * v + a] = (src < 4) ? x[3 * id[src] + a] : E[src - 4][4 + a];
             }
             sface[sp] = f + 1;
             ++sp;
