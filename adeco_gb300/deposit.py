@@ -285,25 +285,56 @@ def leaf_bbox(node):
                     dtype=np.float32)
 
 
+def leaf_file_name(info: OctreeInfo, q, leaf_dims):
+    """``node_<level>_<ix>_<iy>_<iz>`` of leaf q: its origin in cells of its own
+    level from the root's corner (src/AdOctreeGridWriter.h:104-123)."""
+    root, nd = info.nodes[0], info.nodes[info.leaves[q]]
+    cell = float(nd["ext"]) / leaf_dims
+    io = [int(np.rint((float(nd["min"][a]) - float(root["min"][a])) / cell)) for a in range(3)]
+    return f"node_{int(nd['level'])}_{io[0]}_{io[1]}_{io[2]}", io
+
+
 def write_leaf_files(out_dir, info: OctreeInfo, grids, leaf_dims):
     """``write_patch`` (src/AdOctreeGridWriter.h:67-144): float32 density per leaf
-    into ``node_<level>_<ix>_<iy>_<iz>`` (offsets in cells of the leaf's level).
-    Returns the total mass."""
+    into ``node_<level>_<ix>_<iy>_<iz>``, then the index ``write_meta_data``
+    would write.  Returns the total mass."""
     os.makedirs(out_dir, exist_ok=True)
-    root = info.nodes[0]
     total = 0.0
+    masses = []
     for q, nid in enumerate(info.leaves):
         nd = info.nodes[nid]
-        ext = float(nd["ext"])
-        cell = ext / leaf_dims
+        cell = float(nd["ext"]) / leaf_dims
         inv_cell_vol = 1.0 / (cell * cell * cell)
         g = grids[q].reshape(-1)
-        total += float(g.sum())
-        dens = (g * inv_cell_vol).astype(np.float32)
-        io = [int(np.rint((float(nd["min"][a]) - float(root["min"][a])) / cell)) for a in range(3)]
-        name = os.path.join(out_dir, f"node_{int(nd['level'])}_{io[0]}_{io[1]}_{io[2]}")
-        dens.tofile(name)
+        m = float(g.sum())
+        masses.append(m)
+        total += m
+        name, _ = leaf_file_name(info, q, leaf_dims)
+        (g * inv_cell_vol).astype(np.float32).tofile(os.path.join(out_dir, name))
+    write_meta_data(out_dir, info, leaf_dims, masses)
     return total
+
+
+def write_meta_data(out_dir, info: OctreeInfo, leaf_dims, masses=None, filename="octree_meta.json"):
+    """The leaf index the reference declares but leaves empty (``write_meta_data``,
+    src/AdOctreeGridWriter.h:58-64): the root box, the leaf resolution and, per
+    leaf in getLeafNodes order, its file name, level, integer origin, FP32
+    corner and extent and deposited mass.  JSON, so any reader can find a
+    leaf's file and place its cells."""
+    import json
+    root = info.nodes[0]
+    leaves = []
+    for q, nid in enumerate(info.leaves):
+        nd = info.nodes[nid]
+        name, io = leaf_file_name(info, q, leaf_dims)
+        leaves.append({"file": name, "node": int(nid), "level": int(nd["level"]), "origin_cells": io,
+                       "min": [float(v) for v in nd["min"]], "ext": float(nd["ext"]),
+                       "mass": None if masses is None else float(masses[q])})
+    meta = {"format": "float32 density (mass / cell volume), x fastest", "leaf_dims": int(leaf_dims),
+            "root_min": [float(v) for v in root["min"]], "root_ext": float(root["ext"]),
+            "levels": int(info.levels), "leaves": leaves}
+    with open(os.path.join(out_dir, filename), "w") as f:
+        json.dump(meta, f, indent=1)
 
 
 def deposit_workflow(positions, *, max_tets_per_octree_node, max_refinement_level, linear_patch_resolution=16,

@@ -53,3 +53,32 @@ def test_cpp_wrapper_header_compiles(tmp_path):
     r = subprocess.run(["g++", "-std=c++11", "-fsyntax-only", "-I", os.path.join(ROOT, "include"), str(src)],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_leaf_writer_files_and_meta(tmp_path):
+    """write_leaf_files: one float32 density file per leaf, named by level and
+    integer origin as write_patch names them, plus the JSON leaf index."""
+    import json
+    import numpy as np
+    from adeco_gb300.deposit import OctreeInfo, write_leaf_files
+    dt = np.dtype([("min", "<f4", 3), ("ext", "<f4"), ("level", "<i4"), ("parent", "<i4"), ("first_child", "<i4"),
+                   ("n_meta", "<i4"), ("estimate", "<u8")])
+    nodes = np.zeros(9, dt)
+    nodes[0] = ((0.0, 0.0, 0.0), 8.0, 0, -1, 1, 0, 0)
+    for q in range(8):
+        i, j, k = q & 1, (q >> 1) & 1, q >> 2
+        nodes[1 + q] = ((4.0 * i, 4.0 * j, 4.0 * k), 4.0, 1, 0, -1, 0, 0)
+    info = OctreeInfo(nodes=nodes, leaves=np.arange(8, 0, -1), levels=2)
+    d = 4
+    grids = np.arange(8 * d ** 3, dtype=np.float64).reshape(8, d, d, d)
+    total = write_leaf_files(str(tmp_path), info, grids, d)
+    assert total == grids.sum()
+    meta = json.load(open(tmp_path / "octree_meta.json"))
+    assert meta["leaf_dims"] == d and len(meta["leaves"]) == 8
+    for q, leaf in enumerate(meta["leaves"]):
+        nd = nodes[info.leaves[q]]
+        expect = [int(nd["min"][a] / 1.0) for a in range(3)]        # cell = 4 / 4 = 1
+        assert leaf["origin_cells"] == expect and leaf["file"] == "node_1_%d_%d_%d" % tuple(expect)
+        data = np.fromfile(tmp_path / leaf["file"], np.float32)
+        assert np.allclose(data, grids[q].reshape(-1) / 1.0)          # density = mass / 1^3
+        assert leaf["mass"] == grids[q].sum()
