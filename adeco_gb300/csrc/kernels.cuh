@@ -49,7 +49,12 @@ struct DepositParams {
     double *out_d;                    // FP64 grids (plain path)
     int *counter;                     // persistent work counter
     unsigned long long *stats;        // kNumStats counters or nullptr
-    int *error;                       // device error flag
+    int *error;                       // device error flag (bit 0: tet too large, bit 2: route list full)
+    // ill-conditioned tets, deposited by a second launch (route_fp64_kernel):
+    // entries item << 16 | (cube slot * 6 + tet), count in *route_count
+    unsigned long long *route;
+    unsigned long long *route_count;
+    unsigned long long route_cap;
 };
 
 enum Stat : int {
@@ -738,26 +743,16 @@ __global__ void __launch_bounds__(kThreads, 3) deposit_mixed_kernel(DepositParam
                 np += __popc(bal);
                 __syncwarp();
             }
-            // ill-conditioned tets of this group: whole warp, FP64
-            while (fp64_tets) {
-                const int src = __ffs(fp64_tets) - 1;
-                fp64_tets &= fp64_tets - 1;
-                const int tid64 = W.tetid[src];
-                float3 v[4];
-                load_tet(S.vert, vx, vy, S.cubes[tid64 / 6], tid64 % 6, P.order, cvx, cvy, v);
-                if (vol6_sign_ref(vol6_exact(v[0], v[1], v[2], v[3])) < 0) {
-                    const float3 t = v[0];
-                    v[0] = v[3];
-                    v[3] = t;
-                }
-                int lo[3], hi[3];
-                if (!candidate_range(v, g, lo, hi) || !tile_clamp(g, lo, hi)) continue;
-                unsigned c64 = 0, p64 = 0;
-                deposit_tet_fp64_warp<true>(v, lo, hi, g, P.out, nullptr, c64, p64);
-                st_cand += c64;
-                st_part += p64;
-                st_fp64 += c64;
+            // ill-conditioned tets of this group are listed for route_fp64_kernel:
+            // calling their (large) routine from here made the whole loop spill
+            if (route64) {
+                const unsigned long long k = atomicAdd(P.route_count, 1ull);
+                if (k < P.route_cap)
+                    P.route[k] = ((unsigned long long)item << 16) | (unsigned long long)(S.cubes[tid / 6] * 6 + tid % 6);
+                else
+                    atomicOr(P.error, 4);
             }
+            (void)fp64_tets;
             __syncwarp();
         }
         __syncthreads();
@@ -832,6 +827,58 @@ __global__ void __launch_bounds__(kThreads) deposit_plain_fp64_kernel(DepositPar
             deposit_tet_fp64_warp<false>(v, lo, hi, g, nullptr, P.out_d, nc, np);
         }
     }
+}
+
+// -------------------------------------------------- ill-conditioned tets
+// The tets deposit_mixed_kernel listed (kappa > kKappaFp64), one warp each:
+// vertices re-read from the source, FP64 planes, barycentric FP32 clipping.
+__global__ void __launch_bounds__(kThreads) route_fp64_kernel(DepositParams P)
+{
+    const int lane = threadIdx.x & 31;
+    const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    const unsigned long long count = *P.route_count;
+    const unsigned long long n = count < P.route_cap ? count : P.route_cap;
+    unsigned cand = 0, part = 0;
+    for (unsigned long long e = warp; e < n; e += nwarps) {
+        const unsigned long long entry = P.route[e];
+        const Item it = P.items[entry >> 16];
+        const int local = (int)(entry & 0xffff), c = local / 6, t = local % 6;
+        const int vx = it.nv & 0xff, vy = (it.nv >> 8) & 0xff;
+        const int cvx = vx - 1, cvy = vy - 1;
+        const int ci = c % cvx, r = c / cvx, cj = r % cvy, ck = r / cvy;
+        float3 v[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int3 o = corner_offset(P.order, tet_conn(t, q));
+            const long long gi = it.base + (ci + o.x) + P.stride_y * (cj + o.y) + P.stride_z * (ck + o.z);
+            if (P.src_kind == SRC_LATTICE_F4) {
+                const float4 p = __ldg(reinterpret_cast<const float4 *>(P.src) + gi);
+                v[q] = make_float3(p.x, p.y, p.z);
+            } else {
+                const float *s = reinterpret_cast<const float *>(P.src) + 3 * gi;
+                v[q] = make_float3(__ldg(s), __ldg(s + 1), __ldg(s + 2));
+            }
+        }
+        if (vol6_sign_ref(vol6_exact(v[0], v[1], v[2], v[3])) < 0) {
+            const float3 tmp = v[0];
+            v[0] = v[3];
+            v[3] = tmp;
+        }
+        const GridDesc &g = P.grids[it.grid];
+        int lo[3], hi[3];
+        if (!candidate_range(v, g, lo, hi) || !tile_clamp(g, lo, hi)) continue;
+        unsigned c64 = 0, p64 = 0;
+        deposit_tet_fp64_warp<true>(v, lo, hi, g, P.out, nullptr, c64, p64);
+        cand += c64;
+        part += p64;
+    }
+    if (P.stats) {
+        warp_stat(P.stats, ST_CAND, cand);
+        warp_stat(P.stats, ST_PARTIAL, part);
+        warp_stat(P.stats, ST_FP64, cand);
+    }
+    (void)lane;
 }
 
 // ------------------------------------------- parity / diagnostics kernels

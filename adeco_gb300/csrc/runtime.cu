@@ -163,14 +163,41 @@ struct LaunchStats {
     uint64_t launches = 0;
 };
 
-// One persistent launch of the mixed kernel over `n_items` items.
+// Entries of the list of ill-conditioned tets a mixed launch over n_items
+// items may fill (count word + entries; 8 bytes each): a quarter of a tet per
+// item on average, at least 64K, at most 64M.
+static unsigned long long route_capacity(long long n_items)
+{
+    return (unsigned long long)std::min<long long>(1LL << 26, std::max<long long>(65536, n_items * 256));
+}
+
+// Points P at a route list buffer of route_capacity(...) + 1 words.
+static void set_route(DepositParams &P, unsigned long long *buf, unsigned long long cap)
+{
+    P.route_count = buf;
+    P.route = buf + 1;
+    P.route_cap = cap;
+}
+
+// Message for the device error flag of a mixed launch.
+static int deposit_error(int err, const char *where)
+{
+    if (err & 4) return fail(ADECO_ERR_LIMIT, "more ill-conditioned tets in %s than the route list holds", where);
+    return fail(ADECO_ERR_LIMIT, "a tet spans more than 2^25 candidate cells of %s", where);
+}
+
+// One persistent launch of the mixed kernel over `n_items` items, then the
+// launch that deposits the ill-conditioned tets it listed.
 int launch_mixed(const DeviceProps &dp, DepositParams P, int acc_fp64, cudaStream_t st)
 {
     if (P.n_items <= 0) return ADECO_OK;
     CUDA_TRY(cudaMemsetAsync(P.counter, 0, sizeof(int), st));
+    CUDA_TRY(cudaMemsetAsync(P.route_count, 0, sizeof(unsigned long long), st));
     const int grid = std::max(1, std::min(P.n_items, dp.sms * dp.mixed_blocks_per_sm));
     (void)acc_fp64;  // piece volumes are summed exactly in fixed point
     deposit_mixed_kernel<<<grid, kThreads, dp.mixed_smem, st>>>(P);
+    CUDA_TRY(cudaGetLastError());
+    route_fp64_kernel<<<dp.sms * 4, kThreads, 0, st>>>(P);
     CUDA_TRY(cudaGetLastError());
     return ADECO_OK;
 }
@@ -275,7 +302,10 @@ static int deposit_device_core(int dev, const float *d_pos, size_t patch_offset,
     DevBuf<GridDesc> d_grid;
     DevBuf<int> d_counter;
     DevBuf<long long> d_cube_off;
+    DevBuf<unsigned long long> d_route;
+    const unsigned long long rcap = route_capacity((long long)items.size());
     if ((rc = d_items.reserve(items.size())) || (rc = d_grid.reserve(1)) || (rc = d_counter.reserve(2))) return rc;
+    if (precision != ADECO_PREC_FP64 && (rc = d_route.reserve(rcap + 1))) return rc;
     CUDA_TRY(cudaMemsetAsync(d_counter.p, 0, 2 * sizeof(int), st));
     CUDA_TRY(cudaMemcpyAsync(d_items.p, items.data(), items.size() * sizeof(Item), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(d_grid.p, &g, sizeof g, cudaMemcpyHostToDevice, st));
@@ -294,6 +324,7 @@ static int deposit_device_core(int dev, const float *d_pos, size_t patch_offset,
     P.out_d = d_f64;
     P.counter = d_counter.p;
     P.error = d_counter.p + 1;
+    if (precision != ADECO_PREC_FP64) set_route(P, d_route.p, rcap);
     if (precision == ADECO_PREC_FP64) {
         if ((rc = d_cube_off.reserve(cube_off.size()))) return rc;
         CUDA_TRY(cudaMemcpyAsync(d_cube_off.p, cube_off.data(), cube_off.size() * sizeof(long long),
@@ -306,7 +337,7 @@ static int deposit_device_core(int dev, const float *d_pos, size_t patch_offset,
     int err = 0;
     CUDA_TRY(cudaMemcpyAsync(&err, d_counter.p + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
-    if (err) return fail(ADECO_ERR_LIMIT, "a tet spans more than 2^25 candidate cells of the grid");
+    if (err) return deposit_error(err, "the grid");
     return ADECO_OK;
 }
 
@@ -474,6 +505,8 @@ struct adeco_session {
     DevBuf<double> d_out;
     DevBuf<int> d_counter;
     DevBuf<unsigned long long> d_stats;
+    DevBuf<unsigned long long> d_route;  // ill-conditioned tets of a leaf deposit
+    unsigned long long route_cap = 0;
     DevBuf<long long> d_cube_off;
     std::vector<long long> cube_off;
     size_t out_values = 0;
@@ -795,9 +828,10 @@ extern "C" int adeco_session_build_octree(adeco_session *s, const float *box6, c
     s->cube_off.push_back(cubes);
     int rc;
     s->out_values = nl * (size_t)cells;
+    s->route_cap = route_capacity((long long)s->leaf_items.size());
     if ((rc = s->d_items.reserve(s->leaf_items.size())) || (rc = s->d_grids.reserve(nl)) ||
         (rc = s->d_fixed.reserve(s->out_values)) || (rc = s->d_out.reserve(s->out_values)) ||
-        (rc = s->d_cube_off.reserve(s->cube_off.size())))
+        (rc = s->d_cube_off.reserve(s->cube_off.size())) || (rc = s->d_route.reserve(s->route_cap + 1)))
         return rc;
     CUDA_TRY(cudaMemcpyAsync(s->d_items.p, s->leaf_items.data(), s->leaf_items.size() * sizeof(Item),
                              cudaMemcpyHostToDevice, s->stream));
@@ -883,6 +917,7 @@ static DepositParams session_params(adeco_session *s, bool stats)
     P.counter = s->d_counter.p;
     P.error = s->d_counter.p + 1;
     P.stats = stats ? s->d_stats.p : nullptr;
+    set_route(P, s->d_route.p, s->route_cap);
     return P;
 }
 
@@ -955,7 +990,7 @@ extern "C" int adeco_session_deposit_leaves(adeco_session *s, int precision, dou
     CUDA_TRY(cudaMemcpy(&err, s->d_counter.p + 1, sizeof(int), cudaMemcpyDeviceToHost));
     if (err) {
         cudaMemset(s->d_counter.p + 1, 0, sizeof(int));
-        return fail(ADECO_ERR_LIMIT, "a tet spans more than 2^25 candidate cells of a leaf grid");
+        return deposit_error(err, "a leaf grid");
     }
     float k_ms = 0.f, t_ms = 0.f;
     CUDA_TRY(cudaEventElapsedTime(&k_ms, e0, e1));
@@ -1088,6 +1123,7 @@ struct adeco_session::Batch {
     DevBuf<GridDesc> d_grids;
     DevBuf<unsigned long long> d_fixed;
     DevBuf<int> d_counter;
+    DevBuf<unsigned long long> d_route;
     std::chrono::steady_clock::time_point t_submit;
     double latency_ms = -1.0;
     int n_items = 0;
@@ -1187,8 +1223,9 @@ extern "C" int adeco_session_submit(adeco_session *s, const adeco_request *reqs,
         return fail(ADECO_ERR_MEMORY, "batch needs %.0f bytes, admission budget %.0f", need,
                     s->hbm_fraction * (double)free_b);
     int rc;
+    const unsigned long long rcap = route_capacity((long long)items.size());
     if ((rc = b->d_items.reserve(items.size())) || (rc = b->d_grids.reserve(b->grids.size())) ||
-        (rc = b->d_fixed.reserve(b->cells)) || (rc = b->d_counter.reserve(2)))
+        (rc = b->d_fixed.reserve(b->cells)) || (rc = b->d_counter.reserve(2)) || (rc = b->d_route.reserve(rcap + 1)))
         return rc;
     CUDA_TRY(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
     CUDA_TRY(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming));
@@ -1212,6 +1249,7 @@ extern "C" int adeco_session_submit(adeco_session *s, const adeco_request *reqs,
     P.out = b->d_fixed.p;
     P.counter = b->d_counter.p;
     P.error = b->d_counter.p + 1;
+    set_route(P, b->d_route.p, rcap);
     CUDA_TRY(cudaEventRecord(b->t0, b->stream));
     if ((rc = launch_mixed(s->dp, P, s->acc_fp64, b->stream))) return rc;
     CUDA_TRY(cudaEventRecord(b->t1, b->stream));
@@ -1384,8 +1422,8 @@ extern "C" int adeco_probe_fp32_tflops(int device, double *tflops)
 // adeco_deposit_tets_device for callers that cannot allocate device memory
 // (code running inside a CUDA-graph capture they do not own, a host that
 // forbids cudaMalloc after start-up, a pool allocator owned by someone else).
-// Its scratch -- work counter, error flag, grid descriptor, work items and
-// the 64-bit fixed-point accumulators -- lives in one file-scope device
+// Its scratch -- work counter, error flag, grid descriptor, work items, the
+// 64-bit fixed-point accumulators and the list of ill-conditioned tets -- lives in one file-scope device
 // array of kNoAllocScratchBytes that every GPU loading this library holds
 // until the process exits.  The array is shared by every call on a device and
 // keeps the last call's contents; each call clears what must start at zero.
@@ -1395,8 +1433,10 @@ namespace {
 constexpr int kNoAllocMaxItems = 16384;             // patch sub-blocks of <= 7^3 cubes
 constexpr long long kNoAllocMaxCells = 96LL * 96 * 96;  // grid cells (dims <= 96 for a cube)
 constexpr size_t kNoAllocHeader = 512;               // counter, error flag, GridDesc
-constexpr size_t kNoAllocScratchBytes =
-    kNoAllocHeader + (size_t)kNoAllocMaxItems * sizeof(Item) + (size_t)kNoAllocMaxCells * sizeof(unsigned long long);
+constexpr unsigned long long kNoAllocRouteCap = 65536;  // ill-conditioned tets per call
+constexpr size_t kNoAllocScratchBytes = kNoAllocHeader + (size_t)kNoAllocMaxItems * sizeof(Item) +
+                                        (size_t)kNoAllocMaxCells * sizeof(unsigned long long) +
+                                        (size_t)(kNoAllocRouteCap + 1) * sizeof(unsigned long long);
 }  // namespace
 
 static_assert(256 + sizeof(GridDesc) <= kNoAllocHeader, "grid descriptor must fit the scratch header");
@@ -1493,8 +1533,10 @@ extern "C" int adeco_deposit_tets_device_noalloc(const float *d_positions, size_
     Item *items = reinterpret_cast<Item *>(nd.scratch + kNoAllocHeader);
     unsigned long long *fixed =
         reinterpret_cast<unsigned long long *>(nd.scratch + kNoAllocHeader + (size_t)kNoAllocMaxItems * sizeof(Item));
+    unsigned long long *route = fixed + kNoAllocMaxCells;  // count word, then the entries
     const int shift = choose_shift(6.0 * (double)num_patches * (double)m * m * m, tet_mass);
     CUDA_TRY(cudaMemsetAsync(counter, 0, 2 * sizeof(int), st));
+    CUDA_TRY(cudaMemsetAsync(route, 0, sizeof(unsigned long long), st));
     CUDA_TRY(cudaMemsetAsync(fixed, 0, (size_t)ncell * sizeof(unsigned long long), st));
     noalloc_grid_kernel<<<1, 1, 0, st>>>(grid, make_grid(bbox, dims, tet_mass, shift, 0));
     noalloc_items_kernel<<<(unsigned)((n_items + 127) / 128), 128, 0, st>>>(items, (long long)patch_offset,
@@ -1514,14 +1556,17 @@ extern "C" int adeco_deposit_tets_device_noalloc(const float *d_positions, size_
     P.out = fixed;
     P.counter = counter;
     P.error = counter + 1;
+    set_route(P, route, kNoAllocRouteCap);
     const int blocks = (int)std::max(1LL, std::min(n_items, (long long)nd.sms * nd.blocks_per_sm));
     deposit_mixed_kernel<<<blocks, kThreads, sizeof(SharedMixed), st>>>(P);
+    CUDA_TRY(cudaGetLastError());
+    route_fp64_kernel<<<nd.sms * 4, kThreads, 0, st>>>(P);
     CUDA_TRY(cudaGetLastError());
     fixed_accumulate_f64_kernel<<<1024, 256, 0, st>>>(fixed, d_out, ncell, std::ldexp(1.0, -shift));
     CUDA_TRY(cudaGetLastError());
     int err = 0;
     CUDA_TRY(cudaMemcpyAsync(&err, counter + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
-    if (err) return fail(ADECO_ERR_LIMIT, "a tet spans more than 2^25 candidate cells of the grid");
+    if (err) return deposit_error(err, "the grid");
     return ADECO_OK;
 }

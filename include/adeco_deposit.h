@@ -109,7 +109,7 @@ int adeco_deposit_tets_device(const float *d_positions, size_t positions_size, s
  * No counterpart in the reference (its deposit allocates on every call).
  *
  * It allocates nothing: its scratch is one fixed device array of about
- * 7.3 MB compiled into the library, which every GPU that loads the library
+ * 7.8 MB compiled into the library, which every GPU that loads the library
  * holds until the process exits.  Limits: dims^3 <= 96^3 grid cells and
  * num_patches * ceil(m/7)^3 <= 16384 work items; larger calls return
  * ADECO_ERR_LIMIT.  The first call on a device looks the array up with that
