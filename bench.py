@@ -426,7 +426,7 @@ def run_ours(args, rank, ws, local):
         "roofline": roof,
         "cpu_baseline": cpu,
         "e2e": e2e,
-        "gpu_launches": 2 * args.steps,
+        "gpu_launches": 3 * args.steps,  # per step: deposit, ill-conditioned tets, fixed point -> FP64
         "clocks": out["clocks"],
         "plain_fp64": out["plain"],
         "batched_over_plain": (out["value"] / ws / out["plain"]["tets_per_s"]) if out["plain"] else None,
