@@ -21,6 +21,7 @@ ERR_ARGUMENT, ERR_MEMORY = 1, 5
 PREC_MIXED, PREC_FP64 = 0, 1
 ORDER_REF, ORDER_CONFORMING = 0, 1
 FORMAT_SORTED_BY_ID, FORMAT_DARK_SKY = 0, 1
+OCTREE_DEVICE, OCTREE_HOST = 0, 1
 OUT_F32, OUT_F64 = 0, 1
 
 
@@ -83,6 +84,7 @@ _SIGS = {
     "adeco_session_positions": ([_vp, _vp, _sz], _i),
     "adeco_session_bbox": ([_vp, _vp], _i),
     "adeco_session_build_octree": ([_vp, _vp, _vp, C.c_uint64, _i, _i], _i),
+    "adeco_session_set_octree_builder": ([_vp, _i], _i),
     "adeco_session_octree_size": ([_vp, C.POINTER(_i), C.POINTER(_i), C.POINTER(_i)], _i),
     "adeco_session_octree_nodes": ([_vp, C.POINTER(Node), _i], _i),
     "adeco_session_leaves": ([_vp, _vp, _i], _i),

@@ -46,7 +46,7 @@ uint64_t MetaGrid::estimate(uint64_t id, const float box[6]) const
     }
     const float scaled = (float)(6 * cells) * box_volume(ib);
     const float est = scaled / box_volume(m);
-    return (uint64_t)est;
+    return estimate_to_u64(est);
 }
 
 bool Octree::build(const MetaGrid &mg, const float box6[6], const float roi6[6], uint64_t max_tets, int max_level)

@@ -20,6 +20,18 @@ namespace adeco {
 
 constexpr int kMetaCubes = 7;  // lattice cubes per meta-cell edge
 
+// float -> uint64 of an estimate, truncating.  The reference converts
+// implicitly, which is undefined for negative, NaN and huge values (a
+// degenerate meta-cell AABB, or a root box that misses a meta-cell); here
+// those saturate: NaN and values <= 0 give 0, values >= 2^64 give 2^64 - 1,
+// as the device conversion (round toward zero, saturating) does.
+inline uint64_t estimate_to_u64(float est)
+{
+    if (!(est > 0.f)) return 0;
+    if (est >= 18446744073709551616.f) return ~0ull;
+    return (uint64_t)est;
+}
+
 struct MetaGrid {
     int nx = 0, ny = 0, nz = 0;   // lattice vertices
     int cd[3] = {0, 0, 0};        // meta-cells per axis

@@ -490,6 +490,8 @@ struct adeco_session {
     int nx = 0, ny = 0, nz = 0;
     DevBuf<float4> lattice;
     MetaGrid meta;
+    DevBuf<float> d_meta_bbox;  // the meta-cells' AABBs, also on the device (octree builder)
+    int octree_builder = ADECO_OCTREE_DEVICE;
     MetaIndex meta_index;  // built at the first zoom batch
     float bbox6[6] = {0, 0, 0, 0, 0, 0};  // xmin,xmax,ymin,ymax,zmin,zmax
     // octree + leaf deposit state
@@ -559,7 +561,7 @@ static int session_meta_bbox(adeco_session &S, float *bbox6)
 {
     S.meta.init(S.nx, S.ny, S.nz);
     const long long nmc = (long long)S.meta.count();
-    DevBuf<float> d_bb;
+    DevBuf<float> &d_bb = S.d_meta_bbox;
     int rc;
     if ((rc = d_bb.reserve((size_t)nmc * 6))) return rc;
     meta_bbox_kernel<<<(unsigned)((nmc * 32 + 255) / 256), 256, 0, S.stream>>>(S.lattice.p, S.nx, S.ny, S.nz, S.meta.cd[0],
@@ -595,6 +597,7 @@ static int session_finish(adeco_session &S)
 }
 
 #include "readers.cuh"
+#include "octree_device.cuh"
 
 // Reads `path` into the session's lattice (see readers.cuh).
 static int read_particle_file(adeco_session &S, const char *path, int format, int stride, int periodic, float bbox_out[6])
@@ -797,8 +800,13 @@ extern "C" int adeco_session_build_octree(adeco_session *s, const float *box6, c
     // max_tets_per_node = min(global tets / ranks, parameter) (src/AdDepositWorkFlow.h:169), one rank
     const uint64_t total_tets = 6ull * (uint64_t)(s->nx - 1) * (uint64_t)(s->ny - 1) * (uint64_t)(s->nz - 1);
     const uint64_t max_tets = std::min(total_tets, max_tets_per_node);
-    if (!s->tree.build(s->meta, box, roi6, max_tets, max_level))
+    if (s->octree_builder == ADECO_OCTREE_DEVICE) {
+        CUDA_TRY(cudaSetDevice(s->device));
+        const int rc = build_octree_device(s->meta, s->d_meta_bbox.p, box, roi6, max_tets, max_level, s->stream, s->tree);
+        if (rc) return rc;
+    } else if (!s->tree.build(s->meta, box, roi6, max_tets, max_level)) {
         return fail(ADECO_ERR_LIMIT, "octree generation did not terminate");
+    }
     s->leaf_dims = leaf_dims;
     // per-leaf grids and work items (leaf x meta-cell)
     const size_t nl = s->tree.leaves.size();
@@ -841,6 +849,16 @@ extern "C" int adeco_session_build_octree(adeco_session *s, const float *box6, c
                              cudaMemcpyHostToDevice, s->stream));
     CUDA_TRY(cudaStreamSynchronize(s->stream));
     s->has_tree = true;
+    return ADECO_OK;
+}
+
+extern "C" int adeco_session_set_octree_builder(adeco_session *s, int builder)
+{
+    if (!s) return fail(ADECO_ERR_ARGUMENT, "null session");
+    if (builder != ADECO_OCTREE_DEVICE && builder != ADECO_OCTREE_HOST)
+        return fail(ADECO_ERR_ARGUMENT, "unknown octree builder %d", builder);
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->octree_builder = builder;
     return ADECO_OK;
 }
 

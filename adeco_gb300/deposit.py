@@ -190,9 +190,14 @@ class Session:
         _raise(self._lib.adeco_session_bbox(self._h, _ptr(b)))
         return b
 
-    def build_octree(self, max_tets_per_node, max_level, leaf_dims=16, box6=None, roi6=None):
+    def build_octree(self, max_tets_per_node, max_level, leaf_dims=16, box6=None, roi6=None, builder="device"):
+        """generate_tree over the resident lattice; `builder` "device" (default)
+        or "host" says where the per-(node, meta-cell) work runs: both give the
+        same tree."""
         b = None if box6 is None else _f32(box6)
         r = None if roi6 is None else _f32(roi6)
+        which = {"device": L.OCTREE_DEVICE, "host": L.OCTREE_HOST}[builder]
+        _raise(self._lib.adeco_session_set_octree_builder(self._h, which))
         _raise(self._lib.adeco_session_build_octree(self._h, _ptr(b), _ptr(r), int(max_tets_per_node),
                                                     int(max_level), int(leaf_dims)))
         self.leaf_dims = leaf_dims

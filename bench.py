@@ -356,6 +356,18 @@ def run_ours(args, rank, ws, local):
         out["mass"] = {"mixed_total": mixed_total, "tet_count": tets}
         leaf_values = grids.size
         del grids
+        # octree generation: the device builder against the host one (same tree)
+        tree_ms = {}
+        for builder in ("host", "device"):
+            ts = []
+            for _ in range(4):
+                t0 = time.perf_counter()
+                tinfo = s.build_octree(MAX_TETS, MAX_LEVEL, leaf_dims=LEAF, builder=builder)
+                ts.append((time.perf_counter() - t0) * 1e3)
+            tree_ms[builder] = statistics.median(ts[1:])
+            tree_ms[builder + "_nodes"] = tinfo.nodes.copy()
+        tree_ms["same_tree"] = bool(np.array_equal(tree_ms.pop("host_nodes"), tree_ms.pop("device_nodes")))
+        out["octree_build_ms"] = tree_ms
     # e2e through the public C ABI with host buffers (pinned), per step
     e2e = None
     if not args.skip_e2e:
@@ -436,6 +448,7 @@ def run_ours(args, rank, ws, local):
                                  "partial": st["partial_pairs"] / (out["ms_per_step"] * 1e-3)},
         "pair_counts": st,
         "mass": out["mass"],
+        "octree_build_ms": out["octree_build_ms"],
     }
     print(json.dumps(line), flush=True)
     return 0

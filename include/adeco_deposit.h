@@ -175,6 +175,10 @@ typedef struct {
  * the particle AABB); roi6 likewise (NULL or min > max: the whole box). */
 int adeco_session_build_octree(adeco_session *s, const float *box6, const float *roi6,
                                uint64_t max_tets_per_node, int max_level, int leaf_dims);
+/* Where adeco_session_build_octree does its per-(node, meta-cell) work: on the
+ * device (default) or on the host.  Both give the same tree, node for node. */
+enum { ADECO_OCTREE_DEVICE = 0, ADECO_OCTREE_HOST = 1 };
+int adeco_session_set_octree_builder(adeco_session *s, int builder);
 int adeco_session_octree_size(adeco_session *s, int *n_nodes, int *n_leaves, int *n_levels);
 int adeco_session_octree_nodes(adeco_session *s, adeco_node *nodes, int capacity);
 /* leaf ids in Octree::getLeafNodes order and each leaf's meta-cell list */

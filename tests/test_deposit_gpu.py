@@ -188,6 +188,42 @@ def test_octree_topology_and_leaves(adeco, oracle):
         assert abs(grids.sum() - plain.sum()) <= 1e-9 * total + 3e-7 * np.sqrt(total)
 
 
+def _tree(s, builder, max_tets, max_level, box6=None, roi6=None):
+    info = s.build_octree(max_tets, max_level, leaf_dims=8, box6=box6, roi6=roi6, builder=builder)
+    return info.nodes, info.leaves, [s.leaf_meta(q) for q in range(len(info.leaves))]
+
+
+@pytest.mark.parametrize("case", ["zeldovich96", "clustered64", "roi_corner", "small_box", "root_leaf", "level0"])
+def test_octree_device_equals_host(adeco, case):
+    """The device octree builder gives the host builder's tree: every node
+    (boxes, level, parent, first child, meta count, estimate), the leaf order
+    and every leaf's meta-cell list, bit for bit."""
+    from adeco_gb300.synthetic import zeldovich_lattice
+    if case == "clustered64":
+        pos = zeldovich_lattice(64, L=100.0, seed=4, rms_disp=3.0, infall=40)
+    else:
+        pos = zeldovich_lattice(96 if case == "zeldovich96" else 48, L=100.0, seed=0, rms_disp=3.0)
+    n = pos.shape[0]
+    p = pos.reshape(-1, 3)
+    lo, hi = p.min(0), p.max(0)
+    args = {"zeldovich96": (262144 // 8, 8, None, None),
+            "clustered64": (2000, 10, None, None),
+            "roi_corner": (3000, 9, None, np.array([*lo, *(lo + 0.3 * (hi - lo))], np.float32)),
+            "small_box": (3000, 7, np.array([*(lo + 0.2 * (hi - lo)), *(hi - 0.1 * (hi - lo))], np.float32), None),
+            "root_leaf": (6 * n ** 3, 8, None, None),
+            "level0": (100, 0, None, None)}[case]
+    with adeco.Session(pos) as s:
+        nd, ld, md = _tree(s, "device", args[0], args[1], args[2], args[3])
+        nh, lh, mh = _tree(s, "host", args[0], args[1], args[2], args[3])
+    assert len(nd) == len(nh)
+    for f in ("min", "ext", "level", "parent", "first_child", "n_meta", "estimate"):
+        assert np.array_equal(nd[f], nh[f]), f
+    assert np.array_equal(ld, lh)
+    assert all(np.array_equal(a, b) for a, b in zip(md, mh))
+    if case in ("zeldovich96", "clustered64"):
+        assert len(nd) > 8 * 8 + 1  # more than two levels refined
+
+
 def test_total_mass_workload_scale(adeco):
     """Total mass at workload scale: a 96^3 Zel'dovich lattice (5.1M tets).
     Octree leaves: the mixed total equals the plain FP64 total of the same
