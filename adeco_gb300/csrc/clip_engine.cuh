@@ -416,7 +416,7 @@ long long clip_piece_serial(const float p0[12], int face0)
 }
 
 #ifdef __CUDACC__
-constexpr int kPool = 64;    // pieces per warp pool
+constexpr int kPool = 56;    // pieces per warp pool (2 CTAs of 8 warps fit in an SM's shared memory)
 constexpr int kPairs = 128;  // partial pairs per warp list
 
 struct WarpPool {

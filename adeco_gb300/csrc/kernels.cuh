@@ -22,7 +22,12 @@
 
 namespace adeco {
 
-constexpr int kThreads = 128;
+// 8 warps per CTA and 2 CTAs per SM (16 warps, <= 128 registers, 2 x ~115 KB
+// of shared memory): the staged vertex block (20 KB) is shared by 8 warps
+// instead of 4, which leaves room for a fourth warp per scheduler.  Against 3
+// CTAs of 4 warps (12 warps per SM) this is 5.6% faster on a 208^3 lattice;
+// 8 warps per SM is 11% slower.
+constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kMaxVerts = 512;   // 8^3
 constexpr int kMaxCubes = 343;   // 7^3
@@ -622,7 +627,7 @@ __device__ __forceinline__ void clip_list(const DepositParams &P, const GridDesc
 // Persistent: CTAs take work items (grid x vertex block) from a global
 // counter; inside an item the warps take groups of 32 tets from a shared
 // counter, so no warp waits for another until the item is done.
-__global__ void __launch_bounds__(kThreads, 3) deposit_mixed_kernel(DepositParams P)
+__global__ void __launch_bounds__(kThreads, 2) deposit_mixed_kernel(DepositParams P)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SharedMixed &S = *reinterpret_cast<SharedMixed *>(smem_raw);
