@@ -223,6 +223,58 @@ ADECO_HD inline float halfspace_cube_vol6(float G0, float nx, float ny, float nz
     return v;
 }
 
+// ---------------------------------------------------- double-float
+// An FP32 pair hi + lo carrying ~44 bits, at FP32 speed: the barycentric
+// shares below need more than FP32, and FP64 runs at a small fraction of the
+// FP32 rate on this GPU.  Sums use Knuth's error-free TwoSum, products the
+// fma-based TwoProd; results are renormalised so |lo| <= ulp(hi) / 2.
+struct F2 {
+    float hi, lo;
+};
+
+ADECO_HD inline F2 f2_two_sum(float a, float b)  // a + b exactly
+{
+    const float s = a + b;
+    const float bb = s - a;
+    return {s, (a - (s - bb)) + (b - bb)};
+}
+
+ADECO_HD inline F2 f2_norm(float a, float b)  // |a| >= |b| or a == 0
+{
+    const float s = a + b;
+    return {s, b - (s - a)};
+}
+
+ADECO_HD inline F2 f2_add(F2 x, F2 y)
+{
+    const F2 s = f2_two_sum(x.hi, y.hi);
+    return f2_norm(s.hi, s.lo + (x.lo + y.lo));
+}
+
+ADECO_HD inline F2 f2_mul(F2 x, F2 y)
+{
+    const float p = x.hi * y.hi;
+    float e = fmaf(x.hi, y.hi, -p);
+    e = fmaf(x.hi, y.lo, e);
+    e = fmaf(x.lo, y.hi, e);
+    return f2_norm(p, e);
+}
+
+ADECO_HD inline F2 f2_mul_f(F2 x, float y)
+{
+    const float p = x.hi * y;
+    float e = fmaf(x.hi, y, -p);
+    e = fmaf(x.lo, y, e);
+    return f2_norm(p, e);
+}
+
+// 2x2 minor a d - b c
+ADECO_HD inline F2 f2_minor(F2 a, F2 d, F2 b, F2 c)
+{
+    const F2 bc = f2_mul(b, c);
+    return f2_add(f2_mul(a, d), {-bc.hi, -bc.lo});
+}
+
 // ---------------------------------------------------- barycentric clipping
 // Fraction of a tet's volume inside the unit cube, for tets too flat for the
 // FP32 engine.  A flat tet's volume L^2 h, computed from FP32 coordinates as
@@ -234,21 +286,46 @@ ADECO_HD inline float halfspace_cube_vol6(float G0, float nx, float ny, float nz
 // shape; the mass is that share times the tet's exact mass.  Face tests, cut
 // points (snapped onto the face), splits, last-face fractions and the face
 // order are the engine's, on the piece's own coordinates.
-ADECO_HD inline double clip_bary_fraction(const float X[4][3])
+
+// A piece's signed share of the tet: the determinant of its weight
+// differences (weights 1..3 of vertices 1..3 minus those of vertex 0), from
+// exact differences in double-float.  Signed: every piece keeps the tet's
+// orientation, and |det| would round near-degenerate pieces up and bias the
+// sum.
+ADECO_HD inline F2 bary_share(const float *w)
+{
+    F2 d[3][3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) d[j][i] = f2_two_sum(w[4 * (j + 1) + i + 1], -w[i + 1]);
+    const F2 m0 = f2_minor(d[1][1], d[2][2], d[1][2], d[2][1]);
+    const F2 m1 = f2_minor(d[1][0], d[2][2], d[1][2], d[2][0]);
+    const F2 m2 = f2_minor(d[1][0], d[2][1], d[1][1], d[2][0]);
+    const F2 t1 = f2_mul(d[0][1], m1);
+    return f2_add(f2_add(f2_mul(d[0][0], m0), {-t1.hi, -t1.lo}), f2_mul(d[0][2], m2));
+}
+
+constexpr int kBaryRec = 28;  // a barycentric piece: 16 weights (4 per vertex), then 12 coordinates
+
+// The share inside the unit cube of one barycentric piece rec0 whose faces
+// below face0 are already done, clipped serially with a stack.
+ADECO_HD
+#ifdef __CUDA_ARCH__
+__noinline__
+#else
+inline
+#endif
+F2 clip_bary_serial(const float *rec0, int face0_in)
 {
     constexpr int kDepth = 16;
-    constexpr int kRec = 28;  // 16 weights (4 per vertex) + 12 coordinates
+    constexpr int kRec = kBaryRec;
     float stk[kDepth][kRec];
     int sface[kDepth];
-#pragma unroll
-    for (int i = 0; i < 16; ++i) stk[0][i] = (i % 5 == 0) ? 1.f : 0.f;
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-        for (int a = 0; a < 3; ++a) stk[0][16 + 3 * j + a] = X[j][a];
-    sface[0] = 0;
+    for (int i = 0; i < kRec; ++i) stk[0][i] = rec0[i];
+    sface[0] = face0_in;
     int sp = 1;
-    double acc = 0.0;
+    F2 acc = {0.f, 0.f};
     while (sp > 0) {
         --sp;
         float r[kRec];
@@ -261,21 +338,9 @@ ADECO_HD inline double clip_bary_fraction(const float X[4][3])
         const int all_in = b0 & b1 & b2 & b3, any_in = b0 | b1 | b2 | b3;
         const int relevant = (63 >> face0) << face0;
         if ((~any_in) & relevant) continue;  // beyond a face
-        // the piece's share of the tet: the determinant of its weight
-        // differences (weights 1..3), signed -- every piece keeps the tet's
-        // orientation, and taking |det| would round near-degenerate pieces
-        // up and bias the sum
-        double d[3][3];
-#pragma unroll
-        for (int j = 0; j < 3; ++j)
-#pragma unroll
-            for (int i = 0; i < 3; ++i) d[j][i] = (double)w[4 * (j + 1) + i + 1] - (double)w[i + 1];
-        const double share = d[0][0] * (d[1][1] * d[2][2] - d[1][2] * d[2][1]) -
-                             d[0][1] * (d[1][0] * d[2][2] - d[1][2] * d[2][0]) +
-                             d[0][2] * (d[1][0] * d[2][1] - d[1][1] * d[2][0]);
         const int next = (~all_in) & relevant;
         if (!next) {
-            acc += share;
+            acc = f2_add(acc, bary_share(w));
             continue;
         }
 #ifdef __CUDA_ARCH__
@@ -288,7 +353,7 @@ ADECO_HD inline double clip_bary_fraction(const float X[4][3])
         const int mask = ((b0 >> f) & 1) | (((b1 >> f) & 1) << 1) | (((b2 >> f) & 1) << 2) | (((b3 >> f) & 1) << 3);
         const float xa[4] = {x[axis], x[3 + axis], x[6 + axis], x[9 + axis]};
         if ((next >> (f + 1)) == 0) {  // last crossed face: the inside fraction of the piece
-            acc += share * (double)side_fraction(xa[0], xa[1], xa[2], xa[3], mask, plane);
+            acc = f2_add(acc, f2_mul_f(bary_share(w), side_fraction(xa[0], xa[1], xa[2], xa[3], mask, plane)));
             continue;
         }
         // split by face f into 1 or 3 pieces (vertex patterns of split_piece)
@@ -327,6 +392,20 @@ ADECO_HD inline double clip_bary_fraction(const float X[4][3])
         }
     }
     return acc;
+}
+
+// Fraction of the tet X (cell coordinates) inside the unit cube.
+ADECO_HD inline double clip_bary_fraction(const float X[4][3])
+{
+    float rec[kBaryRec];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) rec[i] = (i % 5 == 0) ? 1.f : 0.f;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) rec[16 + 3 * j + a] = X[j][a];
+    const F2 acc = clip_bary_serial(rec, 0);
+    return (double)acc.hi + (double)acc.lo;
 }
 
 constexpr int kVolShift = 56;  // fixed point of 6x piece volumes (each <= 6)
@@ -522,6 +601,226 @@ __device__ __forceinline__ void clip_pairs(WarpPool &pool, int np, Build build, 
                 atomicAdd(reinterpret_cast<unsigned long long *>(&pool.vacc[owner]), (unsigned long long)acc);
                 ++fallbacks;
             }
+        }
+        __syncwarp();
+    }
+    __syncwarp();
+}
+
+// ------------------------------------------- barycentric warp engine
+// clip_pairs for barycentric pieces (kBaryRec floats each): the partial cells
+// of the ill-conditioned tets are listed per warp and clipped with every lane
+// busy, a lane per piece, instead of a lane per cell.  Steps, faces, cut
+// points, children and last-face fractions are clip_bary_serial's; a lane's
+// piece stays in registers (the vertex permutation and the child patterns
+// are selects, not indexed loads).
+constexpr int kBaryPool = 64;  // pieces per warp pool
+constexpr int kBaryList = 64;  // partial cells per warp list
+
+struct BaryPool {
+    float v[kBaryRec][kBaryPool];
+    uint32_t meta[kBaryPool];  // owner | face << 8
+    long long acc[kBaryList];  // share of each listed cell, fixed point 2^kVolShift
+    uint32_t cell[kBaryList];  // the listed cells (the caller's encoding)
+};
+
+// value i (0..3 weights, 4..6 coordinates) of vertex v of a record
+__device__ __forceinline__ float bary_val(const float *r, int v, int i)
+{
+    return i < 4 ? r[4 * v + i] : r[16 + 3 * v + (i - 4)];
+}
+
+// next face of a piece whose faces below face0 are done: 0 beyond a face
+// (dropped), 1 inside the rest (finished), 2 crossing `face` (mask: its
+// vertices inside; last: no later face is crossed)
+__device__ __forceinline__ int bary_step(const float *r, int face0, int &face, int &mask, bool &last)
+{
+    const int b0 = face_bits(r[16], r[17], r[18]), b1 = face_bits(r[19], r[20], r[21]);
+    const int b2 = face_bits(r[22], r[23], r[24]), b3 = face_bits(r[25], r[26], r[27]);
+    const int all_in = b0 & b1 & b2 & b3, any_in = b0 | b1 | b2 | b3;
+    const int relevant = (63 >> face0) << face0;
+    if ((~any_in) & relevant) return 0;
+    const int next = (~all_in) & relevant;
+    if (!next) return 1;
+    face = __ffs(next) - 1;
+    mask = ((b0 >> face) & 1) | (((b1 >> face) & 1) << 1) | (((b2 >> face) & 1) << 2) | (((b3 >> face) & 1) << 3);
+    last = (next >> (face + 1)) == 0;
+    return 2;
+}
+
+__device__ __forceinline__ float bary_last_fraction(const float *r, int f, int mask)
+{
+    const int axis = f >> 1;
+    const float plane = (f & 1) ? 1.f : 0.f;
+    return side_fraction(sel3(axis, r[16], r[17], r[18]), sel3(axis, r[19], r[20], r[21]),
+                         sel3(axis, r[22], r[23], r[24]), sel3(axis, r[25], r[26], r[27]), mask, plane);
+}
+
+// split at face f: P = the vertices in split_perm order (inside first), E =
+// the cut points of the k-pattern's edges (k=1: AB AC AD; k=2: AC AD BC BD;
+// k=3: AD BD CD), each 4 weights + 3 coordinates
+__device__ __forceinline__ void bary_split(const float *r, int f, int mask, float P[4][7], float E[4][7], int &k)
+{
+    const int pm = split_perm(mask);
+    k = split_kin(mask);
+    const int id0 = pm & 3, id1 = (pm >> 2) & 3, id2 = (pm >> 4) & 3, id3 = (pm >> 6) & 3;
+#pragma unroll
+    for (int i = 0; i < 7; ++i) {
+        const float a0 = bary_val(r, 0, i), a1 = bary_val(r, 1, i), a2 = bary_val(r, 2, i), a3 = bary_val(r, 3, i);
+        P[0][i] = sel4(id0, a0, a1, a2, a3);
+        P[1][i] = sel4(id1, a0, a1, a2, a3);
+        P[2][i] = sel4(id2, a0, a1, a2, a3);
+        P[3][i] = sel4(id3, a0, a1, a2, a3);
+    }
+    const int axis = f >> 1;
+    const float plane = (f & 1) ? 1.f : 0.f;
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        const int vi = e == 0 ? 0 : (e == 1 ? (k == 3 ? 1 : 0) : (e == 2 ? (k == 1 ? 0 : (k == 2 ? 1 : 2)) : 1));
+        const int vo = e == 0 ? (k == 1 ? 1 : (k == 2 ? 2 : 3))
+                              : (e == 1 ? (k == 1 ? 2 : 3) : (e == 2 ? (k == 2 ? 2 : 3) : 3));
+        float pin[7], pout[7];
+#pragma unroll
+        for (int i = 0; i < 7; ++i) {
+            pin[i] = sel4(vi, P[0][i], P[1][i], P[2][i], P[3][i]);
+            pout[i] = sel4(vo, P[0][i], P[1][i], P[2][i], P[3][i]);
+        }
+        const float xin = sel3(axis, pin[4], pin[5], pin[6]), xout = sel3(axis, pout[4], pout[5], pout[6]);
+        const float t = fminf(fmaxf((plane - xin) / (xout - xin), 0.f), 1.f);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) E[e][i] = fmaf(t, pout[i] - pin[i], pin[i]);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) E[e][4 + a] = (a == axis) ? plane : fmaf(t, pout[4 + a] - pin[4 + a], pin[4 + a]);
+    }
+}
+
+// vertex v of child c (0..3: P, 4..7: E) for pattern k: clip_bary_serial's table
+__device__ __forceinline__ int bary_src(int k, int c, int v)
+{
+    if (v == 0) return 0;
+    if (c == 0)
+        return v == 1 ? (k == 1 ? 4 : 1) : (v == 2 ? (k == 1 ? 5 : (k == 2 ? 6 : 2)) : (k == 1 ? 6 : (k == 2 ? 7 : 6)));
+    if (c == 1) return v == 1 ? (k == 2 ? 6 : 1) : (v == 2 ? (k == 2 ? 4 : 6) : (k == 2 ? 7 : 5));
+    return v == 1 ? (k == 2 ? 4 : 5) : (v == 2 ? (k == 2 ? 5 : 6) : (k == 2 ? 7 : 4));
+}
+
+// record entry x (0..27) of child c
+__device__ __forceinline__ float bary_child(const float P[4][7], const float E[4][7], int k, int c, int x)
+{
+    const int v = x < 16 ? x >> 2 : (x - 16) / 3;
+    const int i = x < 16 ? (x & 3) : 4 + (x - 16) % 3;
+    const int s = bary_src(k, c, v);
+    return s < 4 ? sel4(s, P[0][i], P[1][i], P[2][i], P[3][i]) : sel4(s - 4, E[0][i], E[1][i], E[2][i], E[3][i]);
+}
+
+__device__ __forceinline__ long long share_fixed(F2 c)
+{
+    return vol_fixed(c.hi) + vol_fixed(c.lo);
+}
+
+// Clip the warp's np listed cells: build(j, r) writes cell j's piece (the
+// tet in the cell's frame with identity weights).  On return pool.acc[0..np)
+// hold the cells' shares of the tet in fixed point 2^kVolShift.
+template <typename Build>
+__device__ __forceinline__ void clip_bary_pairs(BaryPool &pool, int np, Build build, unsigned &fallbacks)
+{
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1;
+    for (int j = lane; j < np; j += 32) pool.acc[j] = 0;
+    __syncwarp();
+    bool valid = false;
+    float r[kBaryRec];
+    int owner = 0, face = 0;
+    int top = 0, next = 0;
+    for (;;) {
+        // refill idle lanes: pool first (last in, first out), then the list
+        const unsigned need = __ballot_sync(0xffffffffu, !valid);
+        const int rank = __popc(need & lt), nneed = __popc(need);
+        if (!valid) {
+            if (rank < top) {
+                const int idx = top - 1 - rank;
+#pragma unroll
+                for (int x = 0; x < kBaryRec; ++x) r[x] = pool.v[x][idx];
+                const uint32_t m = pool.meta[idx];
+                owner = (int)(m & 0xff);
+                face = (int)(m >> 8);
+                valid = true;
+            } else {
+                const int j = next + rank - top;
+                if (j < np) {
+                    build(j, r);
+                    owner = j;
+                    face = 0;
+                    valid = true;
+                }
+            }
+        }
+        const int from_pool = nneed < top ? nneed : top;
+        top -= from_pool;
+        next = min(np, next + (nneed - from_pool));
+        if (!__any_sync(0xffffffffu, valid)) break;
+        __syncwarp();
+        // one step
+        int npush = 0, k = 1;
+        bool split = false;
+        float P[4][7], E[4][7];
+        if (valid) {
+            int f = 0, mask = 0;
+            bool last = false;
+            const int code = bary_step(r, face, f, mask, last);
+            F2 c = {0.f, 0.f};
+            if (code == 2 && !last) {
+                bary_split(r, f, mask, P, E, k);
+                split = true;
+                npush = (k == 1) ? 0 : 2;
+                face = f + 1;
+            } else {
+                if (code == 1) c = bary_share(r);
+                if (code == 2) c = f2_mul_f(bary_share(r), bary_last_fraction(r, f, mask));
+                valid = false;
+            }
+            const long long v = share_fixed(c);
+            if (v) atomicAdd(reinterpret_cast<unsigned long long *>(&pool.acc[owner]), (unsigned long long)v);
+        }
+        // push children 1 and 2 (warp-wide exclusive scan of npush)
+        int incl = npush;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        if (total) {
+            if (top + total <= kBaryPool) {
+                if (npush) {
+                    const int base = top + incl - npush;
+                    const uint32_t m = (uint32_t)owner | ((uint32_t)face << 8);
+#pragma unroll
+                    for (int x = 0; x < kBaryRec; ++x) {
+                        pool.v[x][base] = bary_child(P, E, k, 1, x);
+                        pool.v[x][base + 1] = bary_child(P, E, k, 2, x);
+                    }
+                    pool.meta[base] = m;
+                    pool.meta[base + 1] = m;
+                }
+                top += total;
+            } else if (npush) {  // pool full: finish this lane's extra pieces serially
+                float rec[kBaryRec];
+                F2 acc = {0.f, 0.f};
+#pragma unroll
+                for (int c = 1; c <= 2; ++c) {
+#pragma unroll
+                    for (int x = 0; x < kBaryRec; ++x) rec[x] = bary_child(P, E, k, c, x);
+                    acc = f2_add(acc, clip_bary_serial(rec, face));
+                }
+                atomicAdd(reinterpret_cast<unsigned long long *>(&pool.acc[owner]),
+                          (unsigned long long)share_fixed(acc));
+                ++fallbacks;
+            }
+        }
+        if (split) {
+#pragma unroll
+            for (int x = 0; x < kBaryRec; ++x) r[x] = bary_child(P, E, k, 0, x);
         }
         __syncwarp();
     }

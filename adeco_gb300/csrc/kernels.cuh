@@ -835,16 +835,310 @@ __global__ void __launch_bounds__(kThreads) deposit_plain_fp64_kernel(DepositPar
 }
 
 // -------------------------------------------------- ill-conditioned tets
-// The tets deposit_mixed_kernel listed (kappa > kKappaFp64), one warp each:
-// vertices re-read from the source, FP64 planes, barycentric FP32 clipping.
-__global__ void __launch_bounds__(kThreads) route_fp64_kernel(DepositParams P)
+// Per-warp state of the tet being routed (shared memory, written by lane 0):
+// FP64 planes for the error-band fallback and the row bounds, the FP32
+// vertex pairs hi + lo in the anchor frame, their planes and error band.
+struct RouteTet {
+    double pn[4][3], pd[4], pp[4], pm[4], rnx[4];
+    double f6;
+    float qf[4][3], ql[4][3], fn[4][3], fd[4], bmin[3], bmax[3], tol;
+    int ex[3];
+};
+
+struct RouteWarp {
+    BaryPool pool;
+    RouteTet t;
+};
+
+constexpr size_t kRouteSmem = sizeof(RouteWarp) * kWarps;
+
+__device__ __forceinline__ void route_setup(const float3 v[4], const int lo[3], const int hi[3], const GridDesc &g,
+                                            RouteTet &T)
+{
+    double qd[4][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const double anchor = fma((double)lo[a], g.delta_d[a], g.gmin_d[a]);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const double x = (a == 0) ? (double)v[q].x : ((a == 1) ? (double)v[q].y : (double)v[q].z);
+            qd[q][a] = (x - anchor) * g.scale_d[a];
+        }
+    }
+    T.f6 = g.mass_factor / fabs(vol6_fast<double>(qd[0], qd[1], qd[2], qd[3]));
+    const int fa[4] = {0, 0, 0, 1}, fb[4] = {2, 3, 1, 2}, fc[4] = {1, 2, 3, 3};
+#pragma unroll
+    for (int f = 0; f < 4; ++f) {
+        const double e1x = qd[fb[f]][0] - qd[fa[f]][0], e1y = qd[fb[f]][1] - qd[fa[f]][1],
+                     e1z = qd[fb[f]][2] - qd[fa[f]][2];
+        const double e2x = qd[fc[f]][0] - qd[fa[f]][0], e2y = qd[fc[f]][1] - qd[fa[f]][1],
+                     e2z = qd[fc[f]][2] - qd[fa[f]][2];
+        const double nx = e1y * e2z - e1z * e2y, ny = e1z * e2x - e1x * e2z, nz = e1x * e2y - e1y * e2x;
+        T.pn[f][0] = nx;
+        T.pn[f][1] = ny;
+        T.pn[f][2] = nz;
+        T.pd[f] = nx * qd[fa[f]][0] + ny * qd[fa[f]][1] + nz * qd[fa[f]][2];
+        T.pp[f] = fmax(nx, 0.0) + fmax(ny, 0.0) + fmax(nz, 0.0);
+        T.pm[f] = fmin(nx, 0.0) + fmin(ny, 0.0) + fmin(nz, 0.0);
+        const double nxr = nx * g.rcell[0];
+        T.rnx[f] = nxr != 0.0 ? 1.0 / nxr : 0.0;
+    }
+    float R = 0.f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        T.ex[a] = hi[a] - lo[a] + 1;
+        R = fmaxf(R, (float)T.ex[a]);
+    }
+    float qf[4][3];
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            qf[q][a] = __double2float_rn(qd[q][a]);
+            T.qf[q][a] = qf[q][a];
+            T.ql[q][a] = __double2float_rn(qd[q][a] - (double)qf[q][a]);
+            R = fmaxf(R, fabsf(qf[q][a]));
+        }
+    float tol = 0.f;
+#pragma unroll
+    for (int f = 0; f < 4; ++f) {
+        const float e1x = qf[fb[f]][0] - qf[fa[f]][0], e1y = qf[fb[f]][1] - qf[fa[f]][1],
+                    e1z = qf[fb[f]][2] - qf[fa[f]][2];
+        const float e2x = qf[fc[f]][0] - qf[fa[f]][0], e2y = qf[fc[f]][1] - qf[fa[f]][1],
+                    e2z = qf[fc[f]][2] - qf[fa[f]][2];
+        const float nx = e1y * e2z - e1z * e2y, ny = e1z * e2x - e1x * e2z, nz = e1x * e2y - e1y * e2x;
+        T.fn[f][0] = nx;
+        T.fn[f][1] = ny;
+        T.fn[f][2] = nz;
+        T.fd[f] = nx * qf[fa[f]][0] + ny * qf[fa[f]][1] + nz * qf[fa[f]][2];
+        const float L1 = fmaxf(fmaxf(fabsf(e1x), fabsf(e1y)), fabsf(e1z));
+        const float L2 = fmaxf(fmaxf(fabsf(e2x), fabsf(e2y)), fabsf(e2z));
+        tol = fmaxf(tol, 1.0e-5f * L1 * L2 * (R + 1.f));
+    }
+    T.tol = tol;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        T.bmin[a] = fminf(fminf(qf[0][a], qf[1][a]), fminf(qf[2][a], qf[3][a]));
+        T.bmax[a] = fmaxf(fmaxf(qf[0][a], qf[1][a]), fmaxf(qf[2][a], qf[3][a]));
+    }
+}
+
+// Cell (a, b, k) of the routed tet: 0 outside, 1 holding the whole tet, 2
+// inside the tet, 3 partial -- classify_pair's tests (FP32 planes with an
+// error band, FP64 planes inside it).
+__device__ __forceinline__ int route_classify(const RouteTet &T, const GridDesc &g, int a, int b, int k, unsigned &n64)
+{
+    const float xa = (float)a, xb = (float)b, xk = (float)k;
+    if (!(T.bmin[0] < xa + 1.f && xa < T.bmax[0] && T.bmin[1] < xb + 1.f && xb < T.bmax[1] && T.bmin[2] < xk + 1.f &&
+          xk < T.bmax[2]))
+        return 0;
+    if (T.bmin[0] >= xa && T.bmax[0] <= xa + 1.f && T.bmin[1] >= xb && T.bmax[1] <= xb + 1.f && T.bmin[2] >= xk &&
+        T.bmax[2] <= xk + 1.f)
+        return 1;
+    bool all_in = true, unsure = false;
+#pragma unroll
+    for (int f = 0; f < 4; ++f) {
+        const float nx = T.fn[f][0], ny = T.fn[f][1], nz = T.fn[f][2];
+        const float base = fmaf(nx, xa, fmaf(ny, xb, fmaf(nz, xk, -T.fd[f])));
+        const float pos = fmaxf(nx, 0.f) + fmaxf(ny, 0.f) + fmaxf(nz, 0.f);
+        const float mx = base + pos;
+        const float mn = base + ((nx + ny + nz) - pos);
+        if (mx < -T.tol) return 0;
+        if (mx <= T.tol) unsure = true;
+        if (mn > T.tol) continue;
+        all_in = false;
+        if (mn > -T.tol) unsure = true;
+    }
+    if (!unsure) return all_in ? 2 : 3;
+    ++n64;
+    const double oa = a * g.rcell[0], ob = b * g.rcell[1], ok = k * g.rcell[2];
+    all_in = true;
+    for (int f = 0; f < 4; ++f) {
+        const double base = T.pn[f][0] * oa + T.pn[f][1] * ob + T.pn[f][2] * ok - T.pd[f];
+        if (base + T.pp[f] <= 0.0) return 0;
+        if (!(base + T.pm[f] > 0.0)) all_in = false;
+    }
+    return all_in ? 2 : 3;
+}
+
+// Clip the np partial cells listed in RW.pool (local indices a + ex0 (b +
+// ex1 k)) with the barycentric warp engine and deposit their masses.  One
+// copy of the engine, called from every place a list fills.
+__device__ __noinline__ void route_flush(RouteWarp &RW, const GridDesc &g, const int lo[3], int np,
+                                         unsigned long long *out, unsigned &fallbacks)
 {
     const int lane = threadIdx.x & 31;
+    const RouteTet &T = RW.t;
+    BaryPool &pool = RW.pool;
+    const int ex0 = T.ex[0], ex1 = T.ex[1];
+    clip_bary_pairs(
+        pool, np,
+        [&](int j, float *r) {
+            const uint32_t c = pool.cell[j];
+            const int a = (int)(c % (uint32_t)ex0), rr = (int)(c / (uint32_t)ex0);
+            const int b = rr % ex1, k = rr / ex1;
+#pragma unroll
+            for (int i = 0; i < 16; ++i) r[i] = (i % 5 == 0) ? 1.f : 0.f;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                r[16 + 3 * q + 0] = cell_coord(T.qf[q][0], T.ql[q][0], a, g.drcell[0]);
+                r[16 + 3 * q + 1] = cell_coord(T.qf[q][1], T.ql[q][1], b, g.drcell[1]);
+                r[16 + 3 * q + 2] = cell_coord(T.qf[q][2], T.ql[q][2], k, g.drcell[2]);
+            }
+        },
+        fallbacks);
+    for (int j = lane; j < np; j += 32) {
+        const uint32_t c = pool.cell[j];
+        const int a = (int)(c % (uint32_t)ex0), rr = (int)(c / (uint32_t)ex0);
+        const int b = rr % ex1, k = rr / ex1;
+        const double dm = ldexp((double)pool.acc[j], -kVolShift) * g.mass_factor;
+        const unsigned long long fx = (unsigned long long)llrint(ldexp(dm, g.shift));
+        if (dm > 0.0 && fx)
+            atomicAdd(out + g.out_offset + (lo[0] + a) + (long long)g.dims * ((lo[1] + b) + (long long)g.dims * (lo[2] + k)),
+                      fx);
+    }
+    __syncwarp();
+}
+
+// One ill-conditioned tet, candidate range [lo, hi], deposited by a warp.
+// Cells are offered in warp-wide rounds, at most one per lane: short rows
+// (fewer than 8 cells along x) a cell per lane; long rows a row per lane,
+// where the FP64 plane bounds, linear in the cell index and widened by a cell
+// against rounding, skip the cells certainly outside and fill those certainly
+// inside, and only the cells in between are offered.  Cells holding the tet
+// or inside it are deposited at once; partial cells are listed and, 32 or
+// more at a time, clipped by the barycentric warp engine from the FP32 hi +
+// lo cell coordinates: the share of the tet times its exact mass.
+__device__ __noinline__ void route_tet_warp(const float3 v[4], const int lo[3], const int hi[3], const GridDesc &g,
+                                            unsigned long long *out, RouteWarp &RW, unsigned &n_cand, unsigned &n_part,
+                                            unsigned &n64, unsigned &fallbacks)
+{
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1;
+    RouteTet &T = RW.t;
+    BaryPool &pool = RW.pool;
+    __syncwarp();  // no lane still reads the previous tet's state
+    if (lane == 0) route_setup(v, lo, hi, g, T);
+    __syncwarp();
+    const int ex0 = T.ex[0], ex1 = T.ex[1], ex2 = T.ex[2];
+    const double inside6 = 6.0 * T.f6;
+    auto put = [&](int a, int b, int k, double dm) {
+        const unsigned long long fx = (unsigned long long)llrint(ldexp(dm, g.shift));
+        if (fx)
+            atomicAdd(out + g.out_offset + (lo[0] + a) +
+                          (long long)g.dims * ((lo[1] + b) + (long long)g.dims * (lo[2] + k)),
+                      fx);
+    };
+    int np = 0;  // listed partial cells (the same in every lane)
+    auto flush = [&]() {
+        route_flush(RW, g, lo, np, out, fallbacks);
+        np = 0;
+    };
+    auto offer = [&](bool has, int a, int b, int k) {
+        int cls = 0;
+        if (has) {
+            ++n_cand;
+            cls = route_classify(T, g, a, b, k, n64);
+            if (cls == 1) put(a, b, k, (double)g.tet_mass);
+            if (cls == 2) put(a, b, k, inside6);
+        }
+        const unsigned part = __ballot_sync(0xffffffffu, cls == 3);
+        if (cls == 3) {
+            pool.cell[np + __popc(part & lt)] = (uint32_t)a + (uint32_t)ex0 * ((uint32_t)b + (uint32_t)ex1 * (uint32_t)k);
+            ++n_part;
+        }
+        np += __popc(part);
+        __syncwarp();
+        if (np > kBaryList - 32) flush();
+    };
+    if (ex0 < 8) {
+        const long long ncell = (long long)ex0 * ex1 * ex2;
+        for (long long c0 = 0; c0 < ncell; c0 += 32) {
+            const long long cc = c0 + lane;
+            const bool has = cc < ncell;
+            int a = 0, b = 0, k = 0;
+            if (has) {
+                const long long rr = cc / ex0;
+                a = (int)(cc % ex0);
+                b = (int)(rr % ex1);
+                k = (int)(rr / ex1);
+            }
+            offer(has, a, b, k);
+        }
+    } else {
+        const long long nrows = (long long)ex1 * ex2;
+        long long rr = lane;  // this lane's row
+        int b = 0, k = 0, a = 0, a1 = 0, a2 = 0, a3 = -1;  // cells to offer: [a, a1), then [a2, a3]
+        bool active = false;
+        for (;;) {
+            while (!active && rr < nrows) {
+                b = (int)(rr % ex1);
+                k = (int)(rr / ex1);
+                const double ob = b * g.rcell[1], ok = k * g.rcell[2];
+                double c0 = 0.0, c1 = ex0 - 1, i0 = 0.0, i1 = ex0 - 1;
+                bool none = false, no_in = false;
+#pragma unroll
+                for (int f = 0; f < 4; ++f) {
+                    const double nx = T.pn[f][0];
+                    const double K = T.pn[f][1] * ob + T.pn[f][2] * ok - T.pd[f];
+                    if (nx > 0.0) {
+                        c0 = fmax(c0, floor(-(K + T.pp[f]) * T.rnx[f]) - 1.0);
+                        i0 = fmax(i0, floor(-(K + T.pm[f]) * T.rnx[f]) + 2.0);
+                    } else if (nx < 0.0) {
+                        c1 = fmin(c1, ceil(-(K + T.pp[f]) * T.rnx[f]) + 1.0);
+                        i1 = fmin(i1, ceil(-(K + T.pm[f]) * T.rnx[f]) - 2.0);
+                    } else {
+                        none = none || !(K + T.pp[f] > 0.0);
+                        no_in = no_in || !(K + T.pm[f] > 0.0);
+                    }
+                }
+                if (none) {
+                    rr += 32;
+                    continue;
+                }
+                const int lc = (int)fmax(c0, 0.0), hc = (int)fmin(c1, (double)(ex0 - 1));
+                int li = (int)fmax(i0, (double)lc), hi_ = (int)fmin(i1, (double)hc);
+                if (no_in || li > hi_) {
+                    li = hc + 1;
+                    hi_ = hc;
+                }
+                for (int x = li; x <= hi_; ++x) put(x, b, k, inside6);
+                if (li <= hi_) n_cand += hi_ - li + 1;
+                a = lc;
+                a1 = li;
+                a2 = hi_ + 1;
+                a3 = hc;
+                active = a < a1 || a2 <= a3;
+                if (!active) rr += 32;
+            }
+            if (!__any_sync(0xffffffffu, active)) break;
+            bool has = false;
+            int ca = 0;
+            if (active) {
+                has = true;
+                ca = a < a1 ? a++ : a2++;
+                if (a >= a1 && a2 > a3) {
+                    active = false;
+                    rr += 32;
+                }
+            }
+            offer(has, ca, b, k);
+        }
+    }
+    if (np) flush();
+}
+
+// The tets deposit_mixed_kernel listed (kappa > kKappaFp64), one warp each:
+// vertices re-read from the source, then route_tet_warp.
+__global__ void __launch_bounds__(kThreads, 2) route_fp64_kernel(DepositParams P)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    RouteWarp &RW = reinterpret_cast<RouteWarp *>(smem_raw)[threadIdx.x >> 5];
     const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
     const unsigned long long count = *P.route_count;
     const unsigned long long n = count < P.route_cap ? count : P.route_cap;
-    unsigned cand = 0, part = 0;
+    unsigned cand = 0, part = 0, n64 = 0, fb = 0;
     for (unsigned long long e = warp; e < n; e += nwarps) {
         const unsigned long long entry = P.route[e];
         const Item it = P.items[entry >> 16];
@@ -873,17 +1167,14 @@ __global__ void __launch_bounds__(kThreads) route_fp64_kernel(DepositParams P)
         const GridDesc &g = P.grids[it.grid];
         int lo[3], hi[3];
         if (!candidate_range(v, g, lo, hi) || !tile_clamp(g, lo, hi)) continue;
-        unsigned c64 = 0, p64 = 0;
-        deposit_tet_fp64_warp<true>(v, lo, hi, g, P.out, nullptr, c64, p64);
-        cand += c64;
-        part += p64;
+        route_tet_warp(v, lo, hi, g, P.out, RW, cand, part, n64, fb);
     }
     if (P.stats) {
         warp_stat(P.stats, ST_CAND, cand);
         warp_stat(P.stats, ST_PARTIAL, part);
-        warp_stat(P.stats, ST_FP64, cand);
+        warp_stat(P.stats, ST_FP64, n64);
+        warp_stat(P.stats, ST_FALLBACK, fb);
     }
-    (void)lane;
 }
 
 // ------------------------------------------- parity / diagnostics kernels

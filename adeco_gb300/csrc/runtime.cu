@@ -152,6 +152,7 @@ int mixed_setup(int device, DeviceProps &dp)
     dp.mixed_smem = sizeof(SharedMixed);
     CUDA_TRY(cudaFuncSetAttribute(deposit_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)dp.mixed_smem));
+    CUDA_TRY(cudaFuncSetAttribute(route_fp64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRouteSmem));
     int nb = 0;
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, deposit_mixed_kernel, kThreads, dp.mixed_smem));
     dp.mixed_blocks_per_sm = std::max(1, nb);
@@ -197,7 +198,7 @@ int launch_mixed(const DeviceProps &dp, DepositParams P, int acc_fp64, cudaStrea
     (void)acc_fp64;  // piece volumes are summed exactly in fixed point
     deposit_mixed_kernel<<<grid, kThreads, dp.mixed_smem, st>>>(P);
     CUDA_TRY(cudaGetLastError());
-    route_fp64_kernel<<<dp.sms * 4, kThreads, 0, st>>>(P);
+    route_fp64_kernel<<<dp.sms * 4, kThreads, kRouteSmem, st>>>(P);
     CUDA_TRY(cudaGetLastError());
     return ADECO_OK;
 }
@@ -1487,6 +1488,7 @@ int noalloc_setup(int dev, NoAllocDevice &out)
         CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         CUDA_TRY(cudaFuncSetAttribute(deposit_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)sizeof(SharedMixed)));
+        CUDA_TRY(cudaFuncSetAttribute(route_fp64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRouteSmem));
         CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, deposit_mixed_kernel, kThreads,
                                                                sizeof(SharedMixed)));
         d.scratch = static_cast<unsigned char *>(ptr);
@@ -1578,7 +1580,7 @@ extern "C" int adeco_deposit_tets_device_noalloc(const float *d_positions, size_
     const int blocks = (int)std::max(1LL, std::min(n_items, (long long)nd.sms * nd.blocks_per_sm));
     deposit_mixed_kernel<<<blocks, kThreads, sizeof(SharedMixed), st>>>(P);
     CUDA_TRY(cudaGetLastError());
-    route_fp64_kernel<<<nd.sms * 4, kThreads, 0, st>>>(P);
+    route_fp64_kernel<<<nd.sms * 4, kThreads, kRouteSmem, st>>>(P);
     CUDA_TRY(cudaGetLastError());
     fixed_accumulate_f64_kernel<<<1024, 256, 0, st>>>(fixed, d_out, ncell, std::ldexp(1.0, -shift));
     CUDA_TRY(cudaGetLastError());
