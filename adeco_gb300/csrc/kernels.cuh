@@ -54,7 +54,8 @@ struct DepositParams {
     double *out_d;                    // FP64 grids (plain path)
     int *counter;                     // persistent work counter
     unsigned long long *stats;        // kNumStats counters or nullptr
-    int *error;                       // device error flag (bit 0: tet too large, bit 2: route list full)
+    int *error;                       // device error flag (bit 0: tet too large, bit 2: route list full,
+                                      // bit 3: a work-sharing wait timed out)
     // ill-conditioned tets, deposited by a second launch (route_fp64_kernel):
     // entries item << 16 | (cube slot * 6 + tet), count in *route_count
     unsigned long long *route;
@@ -96,6 +97,13 @@ struct WarpTets {
 // miss the 1e-5 per-cell bar.  Lattice tets sit near kappa = 5.2.
 constexpr float kKappaFp64 = 32.f;
 
+// Work sharing inside an item: pairs per chunk, and the bounded waits (a
+// helper looking for work gives up; an owner waiting for its helpers sets
+// error bit 8 and goes on).
+constexpr int kChunk = 512;
+constexpr unsigned kHelpSpins = 1u << 14;
+constexpr unsigned kCloseSpins = 1u << 26;
+
 struct SharedMixed {
     float4 vert[kMaxVerts];
     float gh[3][kMaxVerts];   // grid-frame coordinates of the staged vertices, hi
@@ -108,6 +116,12 @@ struct SharedMixed {
     WarpTets wt[kWarps];
     uint32_t queue[kWarps][kQueue];
     WarpPool pool[kWarps];
+    // work sharing inside an item: slot w = warp w's current group
+    int slot_total[kWarps];  // its candidate pairs
+    int slot_next[kWarps];   // first pair not yet taken
+    int slot_busy[kWarps];   // helpers inside the slot
+    int slot_open[kWarps];   // 1 while helpers may join
+    int groups_set;  // groups of the item set up (published or kept private)
 };
 
 __device__ __forceinline__ void stat_add(unsigned long long *stats, int which, unsigned long long v)
@@ -624,9 +638,136 @@ __device__ __forceinline__ void clip_list(const DepositParams &P, const GridDesc
 }
 
 // -------------------------------------------------- mixed batched kernel
+// per-thread pair counters
+struct PairStats {
+    unsigned tets = 0, cand = 0, bbox = 0, in = 0, cin = 0, part = 0, fp64 = 0, fb = 0;
+};
+
+// Sets up group grp (tets 32 grp .. 32 grp + 31 of the item's live cubes) in
+// the warp's table W and returns its candidate pairs.  route64: this lane's
+// tet is ill-conditioned (listed by group_route, no pairs here).
+__device__ __forceinline__ int group_setup(const DepositParams &P, const SharedMixed &S, WarpTets &W,
+                                           const GridDesc &g, int grp, int ntet, int vx, int vy, int cvx, int cvy,
+                                           int lane, PairStats &st, bool &route64, int &tid)
+{
+    tid = grp * 32 + lane;
+    int cnt = 0;
+    route64 = false;
+    if (tid < ntet) {
+        float3 v[4];
+        int vid[4];
+        load_tet(S.vert, vx, vy, S.cubes[tid / 6], tid % 6, P.order, cvx, cvy, v, vid);
+        float gh[4][3], gl[4][3];
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                gh[q][a] = S.gh[a][vid[q]];
+                gl[q][a] = S.gl[a][vid[q]];
+            }
+        cnt = setup_tet(v, gh, gl, g, W, lane, P.error, &route64);
+        W.tetid[lane] = tid;
+    }
+    st.tets += (cnt > 0);
+    route64 = route64 && cnt > 0;
+    if (route64) cnt = 0;  // deposited by route_fp64_kernel
+    // exclusive scan of the pair counts across the warp
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    W.scan[lane] = incl - cnt;
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    if (lane == 31) W.scan[32] = total;
+    __syncwarp();
+    return total;
+}
+
+// Ill-conditioned tets are listed for route_fp64_kernel: calling their
+// (large) routine from the pair loop made the whole loop spill.
+__device__ __forceinline__ void group_route(const DepositParams &P, const SharedMixed &S, int item, bool route64,
+                                            int tid)
+{
+    if (route64) {
+        const unsigned long long k = atomicAdd(P.route_count, 1ull);
+        if (k < P.route_cap)
+            P.route[k] = ((unsigned long long)item << 16) | (unsigned long long)(S.cubes[tid / 6] * 6 + tid % 6);
+        else
+            atomicOr(P.error, 4);
+    }
+}
+
+// Candidate pairs [c0, c1) of the group in table Wc, flattened across the
+// warp: classified, inside cells and one-face cells deposited at once,
+// partial cells listed in Q and clipped by the engine (one call site keeps a
+// single copy of it).
+__device__ __forceinline__ void pair_range(const DepositParams &P, const GridDesc &g, const WarpTets &Wc,
+                                           WarpPool &pool, uint32_t *Q, int c0, int c1, int lane, PairStats &st)
+{
+    int np = 0;  // partial pairs listed in Q
+    for (int pb = c0;; pb += 32) {
+        if (np > kQueue - 32 || (pb >= c1 && np)) {
+            clip_list(P, g, Wc, pool, Q, np, st.fb);
+            np = 0;
+        }
+        if (pb >= c1) break;
+        const int pidx = pb + lane;
+        bool part = false;
+        uint32_t entry = 0;
+        if (pidx < c1) {
+            int s = 0;
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1)
+                if (Wc.scan[s + step] <= pidx) s += step;
+            const int local = pidx - Wc.scan[s];
+            const int ex0 = Wc.ex[0][s], ex1 = Wc.ex[1][s];
+            const int a = local % ex0, r = local / ex0, b = r % ex1, c = r / ex1;
+            ++st.cand;
+            bool f64 = false;
+            int cross = -1;
+            const int cls = classify_pair(Wc, g, s, a, b, c, f64, cross);
+            st.fp64 += f64;
+            if (cls == P_TET_INSIDE) {
+                ++st.in;
+                ++st.bbox;
+                scatter(P, g, Wc, s, a, b, c, (double)g.tet_mass);
+            } else if (cls == P_CELL_INSIDE) {
+                ++st.cin;
+                ++st.bbox;
+                scatter(P, g, Wc, s, a, b, c, 6.0 * Wc.factor6[s]);
+            } else if (cls == P_PARTIAL) {
+                ++st.part;
+                ++st.bbox;
+                if (cross >= 0) {  // one face cuts the cell: closed form, no clipping
+                    const double dm = (double)halfspace_pair_vol6(Wc, g, s, a, b, c, cross) * Wc.factor6[s];
+                    if (dm > 0.0) scatter(P, g, Wc, s, a, b, c, dm);
+                } else {
+                    part = true;
+                    entry = ((uint32_t)s << 27) | (uint32_t)local;
+                }
+            }
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, part);
+        if (part) Q[np + __popc(bal & ((1u << lane) - 1))] = entry;
+        np += __popc(bal);
+        __syncwarp();
+    }
+}
+
 // Persistent: CTAs take work items (grid x vertex block) from a global
 // counter; inside an item the warps take groups of 32 tets from a shared
 // counter, so no warp waits for another until the item is done.
+// kShare (zoom batches): a group with more than one chunk of pairs is
+// published in its warp's slot, and warps whose groups are done take chunks
+// of kChunk pairs from open slots instead of waiting for the slowest warp at
+// the end of the item.  On fine grids an item holds few tets with thousands
+// of cells each, and one warp carried most of it (zoom batch 8.19 s without,
+// 6.2 s with).  On coarse grids every group is a single chunk: kShare false
+// keeps the plain loop there, whose registers the slot state would crowd
+// (octree leaves 12% slower with it).
+template <bool kShare>
 __global__ void __launch_bounds__(kThreads, 2) deposit_mixed_kernel(DepositParams P)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -635,13 +776,18 @@ __global__ void __launch_bounds__(kThreads, 2) deposit_mixed_kernel(DepositParam
     WarpTets &W = S.wt[warp];
     uint32_t *Q = S.queue[warp];
     WarpPool &pool = S.pool[warp];
-    unsigned st_tets = 0, st_cand = 0, st_bbox = 0, st_in = 0, st_cin = 0, st_part = 0, st_fp64 = 0, st_fb = 0;
+    PairStats st;
+    if (kShare && threadIdx.x < kWarps) {
+        S.slot_busy[threadIdx.x] = 0;
+        S.slot_open[threadIdx.x] = 0;
+    }
 
     for (;;) {
         if (threadIdx.x == 0) {
             S.item = atomicAdd(P.counter, 1);
             S.n_cubes = 0;
             S.next_group = 0;
+            S.groups_set = 0;
         }
         __syncthreads();
         const int item = S.item;
@@ -661,116 +807,128 @@ __global__ void __launch_bounds__(kThreads, 2) deposit_mixed_kernel(DepositParam
         __syncthreads();
         const int ntet = 6 * S.n_cubes;
         const int ngroups = (ntet + 31) / 32;
-        for (;;) {
-            int grp = 0;
-            if (lane == 0) grp = atomicAdd(&S.next_group, 1);
-            grp = __shfl_sync(0xffffffffu, grp, 0);
-            if (grp >= ngroups) break;
-            const int tid = grp * 32 + lane;
-            int cnt = 0;
-            bool route64 = false;
-            if (tid < ntet) {
-                float3 v[4];
-                int vid[4];
-                load_tet(S.vert, vx, vy, S.cubes[tid / 6], tid % 6, P.order, cvx, cvy, v, vid);
-                float gh[4][3], gl[4][3];
-#pragma unroll
-                for (int q = 0; q < 4; ++q)
-#pragma unroll
-                    for (int a = 0; a < 3; ++a) {
-                        gh[q][a] = S.gh[a][vid[q]];
-                        gl[q][a] = S.gl[a][vid[q]];
-                    }
-                cnt = setup_tet(v, gh, gl, g, W, lane, P.error, &route64);
-                W.tetid[lane] = tid;
-            }
-            st_tets += (cnt > 0);
-            route64 = route64 && cnt > 0;
-            if (route64) cnt = 0;  // deposited below by the FP64 route
-            unsigned fp64_tets = __ballot_sync(0xffffffffu, route64);
-            // exclusive scan of the pair counts across the warp
-            int incl = cnt;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int y = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= o) incl += y;
-            }
-            W.scan[lane] = incl - cnt;
-            const int total = __shfl_sync(0xffffffffu, incl, 31);
-            if (lane == 31) W.scan[32] = total;
-            __syncwarp();
-            int np = 0;  // partial pairs listed in Q
-            for (int pb = 0;; pb += 32) {
-                // one call site keeps a single copy of the clip engine
-                if (np > kQueue - 32 || (pb >= total && np)) {
-                    clip_list(P, g, W, pool, Q, np, st_fb);
-                    np = 0;
-                }
-                if (pb >= total) break;
-                const int pidx = pb + lane;
-                bool part = false;
-                uint32_t entry = 0;
-                if (pidx < total) {
-                    int s = 0;
-#pragma unroll
-                    for (int step = 16; step > 0; step >>= 1)
-                        if (W.scan[s + step] <= pidx) s += step;
-                    const int local = pidx - W.scan[s];
-                    const int ex0 = W.ex[0][s], ex1 = W.ex[1][s];
-                    const int a = local % ex0, r = local / ex0, b = r % ex1, c = r / ex1;
-                    ++st_cand;
-                    bool f64 = false;
-                    int cross = -1;
-                    const int cls = classify_pair(W, g, s, a, b, c, f64, cross);
-                    st_fp64 += f64;
-                    if (cls == P_TET_INSIDE) {
-                        ++st_in;
-                        ++st_bbox;
-                        scatter(P, g, W, s, a, b, c, (double)g.tet_mass);
-                    } else if (cls == P_CELL_INSIDE) {
-                        ++st_cin;
-                        ++st_bbox;
-                        scatter(P, g, W, s, a, b, c, 6.0 * W.factor6[s]);
-                    } else if (cls == P_PARTIAL) {
-                        ++st_part;
-                        ++st_bbox;
-                        if (cross >= 0) {  // one face cuts the cell: closed form, no clipping
-                            const double dm = (double)halfspace_pair_vol6(W, g, s, a, b, c, cross) * W.factor6[s];
-                            if (dm > 0.0) scatter(P, g, W, s, a, b, c, dm);
-                        } else {
-                            part = true;
-                            entry = ((uint32_t)s << 27) | (uint32_t)local;
-                        }
-                    }
-                }
-                const unsigned bal = __ballot_sync(0xffffffffu, part);
-                if (part) Q[np + __popc(bal & ((1u << lane) - 1))] = entry;
-                np += __popc(bal);
+        if (!kShare) {
+            for (;;) {
+                int grp = 0;
+                if (lane == 0) grp = atomicAdd(&S.next_group, 1);
+                grp = __shfl_sync(0xffffffffu, grp, 0);
+                if (grp >= ngroups) break;
+                bool route64;
+                int tid;
+                const int total = group_setup(P, S, W, g, grp, ntet, vx, vy, cvx, cvy, lane, st, route64, tid);
+                pair_range(P, g, W, pool, Q, 0, total, lane, st);
+                group_route(P, S, item, route64, tid);
                 __syncwarp();
             }
-            // ill-conditioned tets of this group are listed for route_fp64_kernel:
-            // calling their (large) routine from here made the whole loop spill
-            if (route64) {
-                const unsigned long long k = atomicAdd(P.route_count, 1ull);
-                if (k < P.route_cap)
-                    P.route[k] = ((unsigned long long)item << 16) | (unsigned long long)(S.cubes[tid / 6] * 6 + tid % 6);
-                else
-                    atomicOr(P.error, 4);
+        } else {
+            int cur = -1;      // slot whose pairs this warp takes (its own: cur == warp)
+            int total = 0;     // pairs of slot cur
+            int own_next = 0;  // own group: next pair if kept private, -1 if published
+            for (;;) {
+                if (cur < 0) {
+                    int grp = 0;
+                    if (lane == 0) grp = atomicAdd(&S.next_group, 1);
+                    grp = __shfl_sync(0xffffffffu, grp, 0);
+                    if (grp < ngroups) {
+                        bool route64;
+                        int tid;
+                        total = group_setup(P, S, W, g, grp, ntet, vx, vy, cvx, cvy, lane, st, route64, tid);
+                        group_route(P, S, item, route64, tid);
+                        // a group of one chunk or less is kept private
+                        const bool pub = total > kChunk;
+                        if (lane == 0) {
+                            if (pub) {
+                                S.slot_total[warp] = total;
+                                S.slot_next[warp] = 0;
+                                __threadfence_block();
+                                *(volatile int *)&S.slot_open[warp] = 1;
+                            }
+                            atomicAdd(&S.groups_set, 1);
+                        }
+                        __syncwarp();
+                        cur = warp;
+                        own_next = pub ? -1 : 0;
+                    } else {
+                        // help: join an open slot with pairs left; leave once every
+                        // group is set up and none has pairs left (bounded wait)
+                        int h = -1, ht = 0;
+                        for (unsigned spin = 0;; ++spin) {
+                            int set = 0;
+                            if (lane == 0) {
+                                // read before the scan: if every group was set up by
+                                // then, the scan sees every slot that still has pairs
+                                set = *(volatile int *)&S.groups_set;
+                                __threadfence_block();
+                                for (int d = 1; d < kWarps && h < 0; ++d) {
+                                    const int w = (warp + d) % kWarps;
+                                    if (*(volatile int *)&S.slot_open[w] &&
+                                        *(volatile int *)&S.slot_next[w] < *(volatile int *)&S.slot_total[w]) {
+                                        atomicAdd(&S.slot_busy[w], 1);
+                                        __threadfence_block();
+                                        if (*(volatile int *)&S.slot_open[w]) {
+                                            __threadfence_block();  // then the owner's table is visible
+                                            h = w;
+                                            ht = *(volatile int *)&S.slot_total[w];
+                                        } else {
+                                            atomicSub(&S.slot_busy[w], 1);
+                                        }
+                                    }
+                                }
+                            }
+                            h = __shfl_sync(0xffffffffu, h, 0);
+                            set = __shfl_sync(0xffffffffu, set, 0);
+                            if (h >= 0 || set >= ngroups || spin > kHelpSpins) break;
+                            __nanosleep(256);
+                        }
+                        if (h < 0) break;
+                        cur = h;
+                        total = __shfl_sync(0xffffffffu, ht, 0);
+                        own_next = -1;
+                    }
+                }
+                // next chunk of slot cur
+                int c0 = own_next;
+                if (own_next >= 0) {
+                    own_next = total;
+                } else {
+                    if (lane == 0) c0 = atomicAdd(&S.slot_next[cur], kChunk);
+                    c0 = __shfl_sync(0xffffffffu, c0, 0);
+                }
+                if (c0 >= total) {
+                    if (lane == 0) {
+                        if (cur != warp) {
+                            atomicSub(&S.slot_busy[cur], 1);
+                        } else if (*(volatile int *)&S.slot_open[warp]) {
+                            // close the slot, then wait for the helpers still reading W
+                            *(volatile int *)&S.slot_open[warp] = 0;
+                            __threadfence_block();
+                            for (unsigned spin = 0; *(volatile int *)&S.slot_busy[warp] != 0; ++spin) {
+                                if (spin > kCloseSpins) {
+                                    atomicOr(P.error, 8);
+                                    break;
+                                }
+                                __nanosleep(32);
+                            }
+                        }
+                    }
+                    __syncwarp();
+                    cur = -1;
+                    continue;
+                }
+                pair_range(P, g, S.wt[cur], pool, Q, c0, min(total, c0 + kChunk), lane, st);
             }
-            (void)fp64_tets;
-            __syncwarp();
         }
         __syncthreads();
     }
     if (P.stats) {
-        warp_stat(P.stats, ST_TETS, st_tets);
-        warp_stat(P.stats, ST_CAND, st_cand);
-        warp_stat(P.stats, ST_BBOX, st_bbox);
-        warp_stat(P.stats, ST_INSIDE, st_in);
-        warp_stat(P.stats, ST_CELLIN, st_cin);
-        warp_stat(P.stats, ST_PARTIAL, st_part);
-        warp_stat(P.stats, ST_FP64, st_fp64);
-        warp_stat(P.stats, ST_FALLBACK, st_fb);
+        warp_stat(P.stats, ST_TETS, st.tets);
+        warp_stat(P.stats, ST_CAND, st.cand);
+        warp_stat(P.stats, ST_BBOX, st.bbox);
+        warp_stat(P.stats, ST_INSIDE, st.in);
+        warp_stat(P.stats, ST_CELLIN, st.cin);
+        warp_stat(P.stats, ST_PARTIAL, st.part);
+        warp_stat(P.stats, ST_FP64, st.fp64);
+        warp_stat(P.stats, ST_FALLBACK, st.fb);
     }
 }
 

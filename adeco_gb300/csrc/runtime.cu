@@ -150,11 +150,13 @@ int mixed_setup(int device, DeviceProps &dp)
     CUDA_TRY(cudaGetDeviceProperties(&prop, device));
     dp.sms = prop.multiProcessorCount;
     dp.mixed_smem = sizeof(SharedMixed);
-    CUDA_TRY(cudaFuncSetAttribute(deposit_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    CUDA_TRY(cudaFuncSetAttribute(deposit_mixed_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)dp.mixed_smem));
+    CUDA_TRY(cudaFuncSetAttribute(deposit_mixed_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)dp.mixed_smem));
     CUDA_TRY(cudaFuncSetAttribute(route_fp64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRouteSmem));
     int nb = 0;
-    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, deposit_mixed_kernel, kThreads, dp.mixed_smem));
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, deposit_mixed_kernel<false>, kThreads, dp.mixed_smem));
     dp.mixed_blocks_per_sm = std::max(1, nb);
     cache[device] = dp;
     return ADECO_OK;
@@ -184,19 +186,24 @@ static void set_route(DepositParams &P, unsigned long long *buf, unsigned long l
 static int deposit_error(int err, const char *where)
 {
     if (err & 4) return fail(ADECO_ERR_LIMIT, "more ill-conditioned tets in %s than the route list holds", where);
+    if (err & 8) return fail(ADECO_ERR_CUDA, "a warp of %s timed out waiting for the warps sharing its pairs", where);
     return fail(ADECO_ERR_LIMIT, "a tet spans more than 2^25 candidate cells of %s", where);
 }
 
 // One persistent launch of the mixed kernel over `n_items` items, then the
-// launch that deposits the ill-conditioned tets it listed.
-int launch_mixed(const DeviceProps &dp, DepositParams P, int acc_fp64, cudaStream_t st)
+// launch that deposits the ill-conditioned tets it listed.  share: warps of
+// an item share the pairs of large tet groups (zoom grids, whose cells are
+// much smaller than the tets).
+int launch_mixed(const DeviceProps &dp, DepositParams P, bool share, cudaStream_t st)
 {
     if (P.n_items <= 0) return ADECO_OK;
     CUDA_TRY(cudaMemsetAsync(P.counter, 0, sizeof(int), st));
     CUDA_TRY(cudaMemsetAsync(P.route_count, 0, sizeof(unsigned long long), st));
     const int grid = std::max(1, std::min(P.n_items, dp.sms * dp.mixed_blocks_per_sm));
-    (void)acc_fp64;  // piece volumes are summed exactly in fixed point
-    deposit_mixed_kernel<<<grid, kThreads, dp.mixed_smem, st>>>(P);
+    if (share)
+        deposit_mixed_kernel<true><<<grid, kThreads, dp.mixed_smem, st>>>(P);
+    else
+        deposit_mixed_kernel<false><<<grid, kThreads, dp.mixed_smem, st>>>(P);
     CUDA_TRY(cudaGetLastError());
     route_fp64_kernel<<<dp.sms * 4, kThreads, kRouteSmem, st>>>(P);
     CUDA_TRY(cudaGetLastError());
@@ -332,7 +339,7 @@ static int deposit_device_core(int dev, const float *d_pos, size_t patch_offset,
                                  cudaMemcpyHostToDevice, st));
         rc = launch_plain(dp, P, d_cube_off.p, 0, cube_off.back(), st);
     } else {
-        rc = launch_mixed(dp, P, 1, st);
+        rc = launch_mixed(dp, P, false, st);
     }
     if (rc) return rc;
     int err = 0;
@@ -945,7 +952,7 @@ static int enqueue_leaves_mixed(adeco_session *s, bool stats)
 {
     const size_t nv = s->out_values;
     CUDA_TRY(cudaMemsetAsync(s->d_fixed.p, 0, nv * sizeof(unsigned long long), s->stream));
-    int rc = launch_mixed(s->dp, session_params(s, stats), s->acc_fp64, s->stream);
+    int rc = launch_mixed(s->dp, session_params(s, stats), false, s->stream);
     if (rc) return rc;
     const long long cells = (long long)s->leaf_dims * s->leaf_dims * s->leaf_dims;
     fixed_to_f64_grids_kernel<<<s->dp.sms * 4, 256, 0, s->stream>>>(s->d_fixed.p, s->d_out.p, s->d_grids.p,
@@ -993,7 +1000,7 @@ extern "C" int adeco_session_deposit_leaves(adeco_session *s, int precision, dou
     } else {
         CUDA_TRY(cudaMemsetAsync(s->d_fixed.p, 0, s->out_values * sizeof(unsigned long long), s->stream));
         CUDA_TRY(cudaEventRecord(e0, s->stream));
-        rc = launch_mixed(s->dp, session_params(s, collect_stats != 0), s->acc_fp64, s->stream);
+        rc = launch_mixed(s->dp, session_params(s, collect_stats != 0), false, s->stream);
         launches = 2;  // the mixed kernel and the ill-conditioned-tet launch
         CUDA_TRY(cudaEventRecord(e1, s->stream));
         const long long cells = (long long)s->leaf_dims * s->leaf_dims * s->leaf_dims;
@@ -1270,7 +1277,7 @@ extern "C" int adeco_session_submit(adeco_session *s, const adeco_request *reqs,
     P.error = b->d_counter.p + 1;
     set_route(P, b->d_route.p, rcap);
     CUDA_TRY(cudaEventRecord(b->t0, b->stream));
-    if ((rc = launch_mixed(s->dp, P, s->acc_fp64, b->stream))) return rc;
+    if ((rc = launch_mixed(s->dp, P, true, b->stream))) return rc;
     CUDA_TRY(cudaEventRecord(b->t1, b->stream));
     CUDA_TRY(cudaEventRecord(b->done, b->stream));
     std::lock_guard<std::mutex> lk(s->mu);
@@ -1486,10 +1493,10 @@ int noalloc_setup(int dev, NoAllocDevice &out)
                         cudaGetErrorString(e));
         int sms = 0, nb = 0;
         CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        CUDA_TRY(cudaFuncSetAttribute(deposit_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        CUDA_TRY(cudaFuncSetAttribute(deposit_mixed_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)sizeof(SharedMixed)));
         CUDA_TRY(cudaFuncSetAttribute(route_fp64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRouteSmem));
-        CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, deposit_mixed_kernel, kThreads,
+        CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, deposit_mixed_kernel<false>, kThreads,
                                                                sizeof(SharedMixed)));
         d.scratch = static_cast<unsigned char *>(ptr);
         d.sms = sms;
@@ -1578,7 +1585,7 @@ extern "C" int adeco_deposit_tets_device_noalloc(const float *d_positions, size_
     P.error = counter + 1;
     set_route(P, route, kNoAllocRouteCap);
     const int blocks = (int)std::max(1LL, std::min(n_items, (long long)nd.sms * nd.blocks_per_sm));
-    deposit_mixed_kernel<<<blocks, kThreads, sizeof(SharedMixed), st>>>(P);
+    deposit_mixed_kernel<false><<<blocks, kThreads, sizeof(SharedMixed), st>>>(P);
     CUDA_TRY(cudaGetLastError());
     route_fp64_kernel<<<nd.sms * 4, kThreads, kRouteSmem, st>>>(P);
     CUDA_TRY(cudaGetLastError());
