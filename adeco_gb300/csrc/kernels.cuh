@@ -606,11 +606,31 @@ __device__ __forceinline__ void pair_piece(const GridDesc &g, const WarpTets &W,
     const int r = local / ex0;
     b = r % ex1;
     c = r / ex1;
+    // Along an axis whose lower face the tet does not reach, the piece is
+    // taken in the cell's mirrored frame, so that the face it crosses lies at
+    // 0: a thin slice under the upper face otherwise lost ~6e-8 cell units per
+    // vertex (5e-5 of a C2 cell's mass; 5e-7 mirrored).  An odd number of
+    // reflections is undone by swapping vertices 0 and 1 (the engine wants a
+    // positively oriented tet).
+    const int cc[3] = {a, b, c};
+    int nflip = 0;
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {
-        p[3 * v + 0] = cell_coord(W.q[3 * v + 0][s], W.qlo[3 * v + 0][s], a, g.drcell[0]);
-        p[3 * v + 1] = cell_coord(W.q[3 * v + 1][s], W.qlo[3 * v + 1][s], b, g.drcell[1]);
-        p[3 * v + 2] = cell_coord(W.q[3 * v + 2][s], W.qlo[3 * v + 2][s], c, g.drcell[2]);
+    for (int x = 0; x < 3; ++x) {
+        const bool flip = W.bmin[x][s] > (float)cc[x];
+        nflip += flip;
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const float hi = W.q[3 * v + x][s], lo = W.qlo[3 * v + x][s];
+            p[3 * v + x] = cell_coord_sel(hi, lo, cc[x], g.drcell[x], flip);
+        }
+    }
+    if (nflip & 1) {
+#pragma unroll
+        for (int x = 0; x < 3; ++x) {
+            const float t = p[x];
+            p[x] = p[3 + x];
+            p[3 + x] = t;
+        }
     }
 }
 
@@ -1137,11 +1157,16 @@ __device__ __noinline__ void route_flush(RouteWarp &RW, const GridDesc &g, const
             const int b = rr % ex1, k = rr / ex1;
 #pragma unroll
             for (int i = 0; i < 16; ++i) r[i] = (i % 5 == 0) ? 1.f : 0.f;
+            // coordinates in the cell's mirrored frame along axes whose lower
+            // face the tet does not reach (as pair_piece); the shares come
+            // from the weights, so no reordering is needed
+            const int cc[3] = {a, b, k};
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                r[16 + 3 * q + 0] = cell_coord(T.qf[q][0], T.ql[q][0], a, g.drcell[0]);
-                r[16 + 3 * q + 1] = cell_coord(T.qf[q][1], T.ql[q][1], b, g.drcell[1]);
-                r[16 + 3 * q + 2] = cell_coord(T.qf[q][2], T.ql[q][2], k, g.drcell[2]);
+            for (int x = 0; x < 3; ++x) {
+                const bool flip = T.bmin[x] > (float)cc[x];
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    r[16 + 3 * q + x] = cell_coord_sel(T.qf[q][x], T.ql[q][x], cc[x], g.drcell[x], flip);
             }
         },
         fallbacks);
