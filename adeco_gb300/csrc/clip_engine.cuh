@@ -394,19 +394,6 @@ F2 clip_bary_serial(const float *rec0, int face0_in)
     return acc;
 }
 
-// Fraction of the tet X (cell coordinates) inside the unit cube.
-ADECO_HD inline double clip_bary_fraction(const float X[4][3])
-{
-    float rec[kBaryRec];
-#pragma unroll
-    for (int i = 0; i < 16; ++i) rec[i] = (i % 5 == 0) ? 1.f : 0.f;
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-        for (int a = 0; a < 3; ++a) rec[16 + 3 * j + a] = X[j][a];
-    const F2 acc = clip_bary_serial(rec, 0);
-    return (double)acc.hi + (double)acc.lo;
-}
 
 constexpr int kVolShift = 56;  // fixed point of 6x piece volumes (each <= 6)
 

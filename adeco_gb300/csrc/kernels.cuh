@@ -331,14 +331,11 @@ enum PairClass : int { P_NO = 0, P_TET_INSIDE = 1, P_CELL_INSIDE = 2, P_PARTIAL 
 
 #ifdef __CUDACC__
 // One positively oriented tet, candidate range [lo, hi], deposited by the
-// whole warp in FP64: lanes stride over the candidate cells, each classified
-// with FP64 face planes and, when partial, clipped in FP64.  kFixed selects
-// the output: 64-bit fixed point (mixed path) or FP64 atomics (plain path).
-// Returns the counts of (candidate, partial) pairs seen by this lane.
-template <bool kFixed>
+// whole warp in FP64 (the plain baseline): lanes stride over the candidate
+// cells, each classified with FP64 face planes and, when partial, clipped in
+// FP64; FP64 atomics.  Counts the (candidate, partial) pairs seen by this lane.
 __device__ __noinline__ void deposit_tet_fp64_warp(const float3 v[4], const int lo[3], const int hi[3], const GridDesc &g,
-                                      unsigned long long *out_fixed, double *out_d, unsigned &n_cand,
-                                      unsigned &n_part)
+                                                   double *out_d, unsigned &n_cand, unsigned &n_part)
 {
     const int lane = threadIdx.x & 31;
     double qd[4][3];
@@ -378,14 +375,7 @@ __device__ __noinline__ void deposit_tet_fp64_warp(const float3 v[4], const int 
         }
     }
     const int ex0 = hi[0] - lo[0] + 1, ex1 = hi[1] - lo[1] + 1, ex2 = hi[2] - lo[2] + 1;
-    auto put = [&](long long idx, double dm) {
-        if (kFixed) {
-            const unsigned long long fx = (unsigned long long)llrint(ldexp(dm, g.shift));
-            if (fx) atomicAdd(out_fixed + idx, fx);
-        } else {
-            atomicAdd(out_d + idx, dm);
-        }
-    };
+    auto put = [&](long long idx, double dm) { atomicAdd(out_d + idx, dm); };
     // one cell, decided exactly in FP64 (bbox, plane bounds, clipping)
     auto cell = [&](int a, int b, int k) {
         ++n_cand;
@@ -417,18 +407,7 @@ __device__ __noinline__ void deposit_tet_fp64_warp(const float3 v[4], const int 
                 p[q][2] = qd[q][2] - ok;
             }
             ++n_part;
-            if (kFixed) {
-                // mixed path: FP32 clipping in the tet's barycentric frame, the
-                // share of the tet times its exact mass
-                float X[4][3];
-#pragma unroll
-                for (int q = 0; q < 4; ++q)
-#pragma unroll
-                    for (int x = 0; x < 3; ++x) X[q][x] = (float)p[q][x];
-                dm = clip_bary_fraction(X) * g.mass_factor;
-            } else {
-                dm = clip_volume6<double, double>(p) * f6;
-            }
+            dm = clip_volume6<double, double>(p) * f6;
         }
         if (!(dm > 0.0)) return;
         put(g.out_offset + (lo[0] + a) + (long long)g.dims * ((lo[1] + b) + (long long)g.dims * (lo[2] + k)), dm);
@@ -1007,7 +986,7 @@ __global__ void __launch_bounds__(kThreads) deposit_plain_fp64_kernel(DepositPar
             if (!candidate_range(v, g, lo, hi) || sgn == 0 || !tile_clamp(g, lo, hi)) continue;
             if (sgn < 0) { const float3 tt = v[0]; v[0] = v[3]; v[3] = tt; }
             unsigned nc = 0, np = 0;
-            deposit_tet_fp64_warp<false>(v, lo, hi, g, nullptr, P.out_d, nc, np);
+            deposit_tet_fp64_warp(v, lo, hi, g, P.out_d, nc, np);
         }
     }
 }
