@@ -59,39 +59,46 @@ def dist_env():
 
 
 class Dist:
-    """Barrier / max-reduce over ranks (torch.distributed, NCCL) for N > 1."""
+    """Barrier / max / sum over ranks (torch.distributed) for N > 1: NCCL on the
+    GPUs, or gloo with CPU tensors (the multi-rank logic tested without a GPU)."""
 
-    def __init__(self, ws, local):
+    def __init__(self, ws, local, backend="nccl"):
         self.ws = ws
         self.pg = None
         if ws > 1:
             import torch
             import torch.distributed as dist
-            torch.cuda.set_device(local)
-            dist.init_process_group("nccl")
+            if backend == "nccl":
+                torch.cuda.set_device(local)
+            dist.init_process_group(backend)
             self.torch, self.dist = torch, dist
+            self.device = "cuda" if backend == "nccl" else "cpu"
 
     def barrier(self):
         if self.ws > 1:
             self.dist.barrier()
 
-    def max(self, x):
-        if self.ws == 1:
-            return x
-        t = self.torch.tensor([x], dtype=self.torch.float64, device="cuda")
-        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+    def _reduce(self, x, op):
+        t = self.torch.tensor([x], dtype=self.torch.float64, device=self.device)
+        self.dist.all_reduce(t, op=op)
         return float(t.item())
 
+    def max(self, x):
+        return x if self.ws == 1 else self._reduce(x, self.dist.ReduceOp.MAX)
+
     def sum(self, x):
-        if self.ws == 1:
-            return x
-        t = self.torch.tensor([x], dtype=self.torch.float64, device="cuda")
-        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
-        return float(t.item())
+        return x if self.ws == 1 else self._reduce(x, self.dist.ReduceOp.SUM)
 
     def close(self):
         if self.ws > 1:
             self.dist.destroy_process_group()
+
+
+def replica_value(dist, tets, ms):
+    """Whole-job throughput of N replicas: all ranks' tets over the slowest
+    rank's time.  Returns (tets/s, max ms)."""
+    ms_max = dist.max(ms)
+    return dist.sum(float(tets)) / (ms_max * 1e-3), ms_max
 
 
 class ClockSampler:
@@ -318,9 +325,7 @@ def run_ours(args, rank, ws, local):
         with ClockSampler(local if ws > 1 else args.device) as clk:
             t = s.replay_leaves(args.steps)
         dist.barrier()
-        ms_step = dist.max(t["kernel_ms"])
-        total_tets = dist.sum(float(tets))
-        out["value"] = total_tets / (ms_step * 1e-3)
+        out["value"], ms_step = replica_value(dist, tets, t["kernel_ms"])
         out["ms_per_step"] = ms_step
         out["clocks"] = clk.summary()
         out["kernel_ms"] = min(kern)
