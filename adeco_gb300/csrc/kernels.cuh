@@ -588,9 +588,9 @@ __device__ __forceinline__ void pair_piece(const GridDesc &g, const WarpTets &W,
     // Along an axis whose lower face the tet does not reach, the piece is
     // taken in the cell's mirrored frame, so that the face it crosses lies at
     // 0: a thin slice under the upper face otherwise lost ~6e-8 cell units per
-    // vertex (5e-5 of a C2 cell's mass; 5e-7 mirrored).  An odd number of
-    // reflections is undone by swapping vertices 0 and 1 (the engine wants a
-    // positively oriented tet).
+    // vertex (up to 5e-5 of such a cell's mass on a 256^3 lattice; 5e-7
+    // mirrored).  An odd number of reflections is undone by swapping vertices
+    // 0 and 1 (the engine wants a positively oriented tet).
     const int cc[3] = {a, b, c};
     int nflip = 0;
 #pragma unroll
