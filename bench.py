@@ -438,7 +438,8 @@ def run_ours(args, rank, ws, local):
         "warmup": args.warmup, "ms_per_step": out["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "tets": tets, "leaves": out["nleaf"], "octree_levels": out["levels"],
-                   "precision": "FP32 clipping; FP64 near-degenerate classification, volume sums, kappa>32 tets; "
+                   "precision": "FP32 clipping in mirrored cell frames (kappa>32 tets: barycentric, double-float shares); "
+                                "FP64 near-degenerate classification and volume normalisers; "
                                 "64-bit fixed-point accumulation",
                    "l2": "inputs larger than L2 (268 MB float4 lattice); no flush", "cuda_graph": True,
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
