@@ -1153,6 +1153,7 @@ struct adeco_session::Batch {
     std::chrono::steady_clock::time_point t_submit;
     double latency_ms = -1.0;
     int n_items = 0;
+    int err = -1;  // the launch's device error flag, read once when a result is first taken
     ~Batch()
     {
         if (done) cudaEventDestroy(done);
@@ -1346,6 +1347,12 @@ extern "C" int adeco_session_result(adeco_session *s, uint64_t batch_id, int ind
     if (index < 0 || index >= (int)b->reqs.size()) return fail(ADECO_ERR_ARGUMENT, "request index out of range");
     int rc = adeco_session_wait(s, batch_id, 3600.0);
     if (rc) return rc;
+    if (b->err < 0) {
+        int err = 0;
+        CUDA_TRY(cudaMemcpy(&err, b->d_counter.p + 1, sizeof(int), cudaMemcpyDeviceToHost));
+        b->err = err;
+    }
+    if (b->err) return deposit_error(b->err, "a zoom grid");
     const size_t n = (size_t)b->reqs[index].dims * b->reqs[index].dims * b->reqs[index].dims;
     if (capacity < n) return fail(ADECO_ERR_ARGUMENT, "capacity %zu < %zu cells", capacity, n);
     std::vector<unsigned long long> tmp(n);
