@@ -574,6 +574,36 @@ __device__ __noinline__ void scatter(const DepositParams &P, const GridDesc &g, 
     atomicAdd(P.out + idx, fx);
 }
 
+// Tet of slot s in the frame of its candidate cell (a, b, c), as the clip
+// engine takes it.  Along an axis whose lower face the tet does not reach,
+// the cell's mirrored frame is used, so that the face it crosses lies at 0:
+// a thin slice under the upper face otherwise lost ~6e-8 cell units per
+// vertex (up to 5e-5 of such a cell's mass on a 256^3 lattice; 5e-7
+// mirrored).  An odd number of reflections is undone by swapping vertices 0
+// and 1 (the engine wants a positively oriented tet).
+ADECO_HD inline void piece_coords(const WarpTets &W, const GridDesc &g, int s, int a, int b, int c, float p[12])
+{
+    const int cc[3] = {a, b, c};
+    int nflip = 0;
+#pragma unroll
+    for (int x = 0; x < 3; ++x) {
+        const bool flip = W.bmin[x][s] > (float)cc[x];
+        nflip += flip;
+#pragma unroll
+        for (int v = 0; v < 4; ++v)
+            p[3 * v + x] = cell_coord_sel(W.q[3 * v + x][s], W.qlo[3 * v + x][s], cc[x], g.drcell[x], flip);
+    }
+    if (nflip & 1) {
+#pragma unroll
+        for (int x = 0; x < 3; ++x) {
+            const float t = p[x];
+            p[x] = p[3 + x];
+            p[3 + x] = t;
+        }
+    }
+}
+
+#ifdef __CUDACC__
 // piece of pair `entry` (slot << 27 | local pair index) in its cell's frame
 __device__ __forceinline__ void pair_piece(const GridDesc &g, const WarpTets &W, uint32_t entry, float p[12], int &s,
                                            int &a, int &b, int &c)
@@ -585,33 +615,9 @@ __device__ __forceinline__ void pair_piece(const GridDesc &g, const WarpTets &W,
     const int r = local / ex0;
     b = r % ex1;
     c = r / ex1;
-    // Along an axis whose lower face the tet does not reach, the piece is
-    // taken in the cell's mirrored frame, so that the face it crosses lies at
-    // 0: a thin slice under the upper face otherwise lost ~6e-8 cell units per
-    // vertex (up to 5e-5 of such a cell's mass on a 256^3 lattice; 5e-7
-    // mirrored).  An odd number of reflections is undone by swapping vertices
-    // 0 and 1 (the engine wants a positively oriented tet).
-    const int cc[3] = {a, b, c};
-    int nflip = 0;
-#pragma unroll
-    for (int x = 0; x < 3; ++x) {
-        const bool flip = W.bmin[x][s] > (float)cc[x];
-        nflip += flip;
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-            const float hi = W.q[3 * v + x][s], lo = W.qlo[3 * v + x][s];
-            p[3 * v + x] = cell_coord_sel(hi, lo, cc[x], g.drcell[x], flip);
-        }
-    }
-    if (nflip & 1) {
-#pragma unroll
-        for (int x = 0; x < 3; ++x) {
-            const float t = p[x];
-            p[x] = p[3 + x];
-            p[3 + x] = t;
-        }
-    }
+    piece_coords(W, g, s, a, b, c, p);
 }
+#endif
 
 // clip the warp's listed partial pairs Q[0..np), then scatter them
 __device__ __forceinline__ void clip_list(const DepositParams &P, const GridDesc &g, const WarpTets &W,
