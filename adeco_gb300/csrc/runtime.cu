@@ -169,7 +169,7 @@ struct LaunchStats {
 // Entries of the list of ill-conditioned tets a mixed launch over n_items
 // items may fill (count word + entries; 8 bytes each): a quarter of a tet per
 // item on average, at least 64K, at most 64M.
-static unsigned long long route_capacity(long long n_items)
+static constexpr unsigned long long route_capacity(long long n_items)
 {
     return (unsigned long long)std::min<long long>(1LL << 26, std::max<long long>(65536, n_items * 256));
 }
@@ -1018,6 +1018,9 @@ extern "C" int adeco_session_deposit_leaves(adeco_session *s, int precision, dou
         cudaMemset(s->d_counter.p + 1, 0, sizeof(int));
         return deposit_error(err, "a leaf grid");
     }
+    unsigned long long routed = 0;  // the mixed launch's route list count
+    if (precision != ADECO_PREC_FP64)
+        CUDA_TRY(cudaMemcpy(&routed, s->d_route.p, sizeof routed, cudaMemcpyDeviceToHost));
     float k_ms = 0.f, t_ms = 0.f;
     CUDA_TRY(cudaEventElapsedTime(&k_ms, e0, e1));
     CUDA_TRY(cudaEventElapsedTime(&t_ms, e0, e2));
@@ -1030,6 +1033,7 @@ extern "C" int adeco_session_deposit_leaves(adeco_session *s, int precision, dou
         timing->total_ms = t_ms;
         timing->launches = launches;
         timing->items = s->leaf_items.size();
+        timing->routed_tets = routed;
         if (collect_stats) {
             unsigned long long st[kNumStats];
             CUDA_TRY(cudaMemcpy(st, s->d_stats.p, sizeof st, cudaMemcpyDeviceToHost));
@@ -1452,26 +1456,30 @@ extern "C" int adeco_probe_fp32_tflops(int device, double *tflops)
 
 // ============================================================ no-allocation entry point
 // adeco_deposit_tets_device_noalloc: the mixed deposit of
-// adeco_deposit_tets_device for callers that cannot allocate device memory
-// (code running inside a CUDA-graph capture they do not own, a host that
-// forbids cudaMalloc after start-up, a pool allocator owned by someone else).
+// adeco_deposit_tets_device for callers that must not allocate device memory
+// while they deposit -- an application that hands all of the GPU's memory to
+// its own pool at start-up, or a latency-critical loop in which cudaMalloc's
+// unbounded time and cudaFree's device-wide synchronisation are not allowed.
 // Its scratch -- work counter, error flag, grid descriptor, work items, the
-// 64-bit fixed-point accumulators and the list of ill-conditioned tets -- lives in one file-scope device
-// array of kNoAllocScratchBytes that every GPU loading this library holds
-// until the process exits.  The array is shared by every call on a device and
-// keeps the last call's contents; each call clears what must start at zero.
-// Calls that overlap on the GPU (two streams, or two host threads) race on
-// it: serialise them.
+// 64-bit fixed-point accumulators and the list of ill-conditioned tets --
+// lives in one file-scope device array of kNoAllocScratchBytes (15.5 MB)
+// that every GPU loading this library holds until the process exits.  The
+// array is shared by every call on a device and keeps the last call's
+// contents; each call clears what must start at zero.  Calls that overlap on
+// the GPU (two streams, or two host threads) race on it: serialise them.
 namespace {
-constexpr int kNoAllocMaxItems = 16384;             // patch sub-blocks of <= 7^3 cubes
+constexpr int kNoAllocMaxItems = 4096;                  // patch sub-blocks of <= 7^3 cubes
 constexpr long long kNoAllocMaxCells = 96LL * 96 * 96;  // grid cells (dims <= 96 for a cube)
-constexpr size_t kNoAllocHeader = 512;               // counter, error flag, GridDesc
-constexpr unsigned long long kNoAllocRouteCap = 65536;  // ill-conditioned tets per call
+constexpr size_t kNoAllocHeader = 512;                  // counter, error flag, GridDesc
+// ill-conditioned tets per call: the allocating path's rule at the item limit,
+// so both paths accept the same calls
+constexpr unsigned long long kNoAllocRouteCap = route_capacity(kNoAllocMaxItems);
 constexpr size_t kNoAllocScratchBytes = kNoAllocHeader + (size_t)kNoAllocMaxItems * sizeof(Item) +
                                         (size_t)kNoAllocMaxCells * sizeof(unsigned long long) +
                                         (size_t)(kNoAllocRouteCap + 1) * sizeof(unsigned long long);
 }  // namespace
 
+static_assert(kNoAllocRouteCap == 1048576ull, "route list of the no-alloc scratch: 2^20 entries");
 static_assert(256 + sizeof(GridDesc) <= kNoAllocHeader, "grid descriptor must fit the scratch header");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
@@ -1590,7 +1598,7 @@ extern "C" int adeco_deposit_tets_device_noalloc(const float *d_positions, size_
     P.out = fixed;
     P.counter = counter;
     P.error = counter + 1;
-    set_route(P, route, kNoAllocRouteCap);
+    set_route(P, route, route_capacity(n_items));  // <= kNoAllocRouteCap, the allocating path's rule
     const int blocks = (int)std::max(1LL, std::min(n_items, (long long)nd.sms * nd.blocks_per_sm));
     deposit_mixed_kernel<false><<<blocks, kThreads, sizeof(SharedMixed), st>>>(P);
     CUDA_TRY(cudaGetLastError());

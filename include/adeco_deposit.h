@@ -37,7 +37,7 @@
 extern "C" {
 #endif
 
-#define ADECO_ABI_VERSION 1
+#define ADECO_ABI_VERSION 2
 
 typedef enum {
     ADECO_OK = 0,
@@ -102,21 +102,26 @@ int adeco_deposit_tets_device(const float *d_positions, size_t positions_size, s
                               size_t num_patches, int meta_cells_per_patch, const float bbox[6], int dims,
                               double *d_out, int precision, int tet_order, double tet_mass, void *stream);
 
-/* Same deposit as adeco_deposit_tets_device (mixed precision only), for
- * callers that cannot allocate device memory at call time: code recorded
- * into a CUDA graph owned by someone else, hosts that forbid cudaMalloc after
- * start-up, or applications whose device memory belongs to their own pool.
+/* Same deposit as adeco_deposit_tets_device (mixed precision only) for
+ * callers that must not allocate device memory while they deposit: an
+ * application that gives all of the GPU's memory to its own pool at start-up
+ * (a cudaMalloc inside the deposit would fail, or take memory the pool
+ * counts on), or a latency-critical loop where cudaMalloc's unbounded time and
+ * cudaFree's device-wide synchronisation are not allowed.
  * No counterpart in the reference (its deposit allocates on every call).
  *
- * It allocates nothing: its scratch is one fixed device array of about
- * 7.8 MB compiled into the library, which every GPU that loads the library
- * holds until the process exits.  Limits: dims^3 <= 96^3 grid cells and
- * num_patches * ceil(m/7)^3 <= 16384 work items; larger calls return
- * ADECO_ERR_LIMIT.  The first call on a device looks the array up with that
- * device current (cudaGetSymbolAddress); make that first call before any
- * stream capture.  Every call shares the array: calls that overlap on the
- * GPU (other streams or host threads) race and must be serialised.
- * d_out is ACCUMULATED (+=); the call synchronises `stream`. */
+ * Arguments: those of adeco_deposit_tets_device without `precision`.
+ * It allocates nothing: its scratch is one fixed device array of 15.5 MB
+ * compiled into the library, which every GPU that loads the library holds
+ * until the process exits.  Limits, each returning ADECO_ERR_LIMIT:
+ * dims^3 <= 96^3 grid cells; num_patches * ceil(m/7)^3 <= 4096 work items;
+ * at most max(65536, 256 * work items) ill-conditioned tets (longest edge
+ * cubed over |6V| above 32) in one call -- the allocating entry point's
+ * limit for the same call.  The first call on a device looks the array up
+ * with that device current (cudaGetSymbolAddress); make that first call
+ * before any stream capture.  Every call shares the array: calls that
+ * overlap on the GPU (other streams or host threads) race and must be
+ * serialised.  d_out is ACCUMULATED (+=); the call synchronises `stream`. */
 int adeco_deposit_tets_device_noalloc(const float *d_positions, size_t positions_size, size_t patch_offset,
                                       size_t num_patches, int meta_cells_per_patch, const float bbox[6], int dims,
                                       double *d_out, int tet_order, double tet_mass, void *stream);
@@ -196,6 +201,8 @@ typedef struct {
     uint64_t tet_inside_pairs;
     uint64_t fp64_pairs;    /* pairs decided by the FP64 plane test                   */
     uint64_t items;         /* work items (grid x vertex block)                       */
+    uint64_t routed_tets;   /* ill-conditioned tets (longest edge^3 > 32 |6V|) that the
+                               barycentric route deposited                          */
 } adeco_timing;
 
 /* Deposit every leaf (leaf_dims^3 cells over the leaf's cube) in one batched

@@ -44,12 +44,17 @@ class Node(C.Structure):
                 ("first_child", C.c_int32), ("pad", C.c_int32), ("estimate", C.c_uint64)]
 
 
-def build(ref: bool = True) -> None:
-    """Compile liboracle.so (and the reference harness when its sources exist)."""
+def build(ref: bool = True, ref_src: str | None = None) -> None:
+    """Compile liboracle.so and, when `ref` is set and the reference's `src/`
+    directory is given (`ref_src`, else the REF_SRC environment variable) and
+    exists, the reference harness."""
     targets = ["all"]
-    if ref and os.path.isdir(os.environ.get("REF_SRC", "/root/reference/src")):
+    src = ref_src or os.environ.get("REF_SRC")
+    extra = []
+    if ref and src and os.path.isdir(src):
         targets.append("ref")
-    subprocess.run(["make", "-s", "-C", HERE] + targets, check=True)
+        extra.append(f"REF_SRC={src}")
+    subprocess.run(["make", "-s", "-C", HERE] + targets + extra, check=True)
 
 
 _lib = None

@@ -57,7 +57,7 @@ def kat_tets():
 
 
 def main():
-    O.build(ref=True)
+    O.build(ref=True, ref_src=os.environ.get("REF_SRC") or "/root/reference/src")
     R = O.ref()
     if R is None:
         raise SystemExit("reference harness missing: run `make -C oracle ref` where the reference exists")

@@ -36,7 +36,7 @@ def test_bindings_cover_every_declared_symbol():
 
 
 def test_abi_version(lib):
-    assert lib.adeco_abi_version() == 1
+    assert lib.adeco_abi_version() == 2
 
 
 def test_last_error_is_empty_string_initially(lib):
