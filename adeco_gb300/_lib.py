@@ -60,6 +60,23 @@ class Timing(C.Structure):
         return {n: (float(getattr(self, n)) if t is C.c_double else int(getattr(self, n))) for n, t in self._fields_}
 
 
+class Tuning(C.Structure):
+    _fields_ = [("zoom_tile", C.c_int), ("share_chunk", C.c_int), ("clip_batch", C.c_int), ("ctas_per_sm", C.c_int),
+                ("route_capacity", C.c_uint64)]
+
+    def as_dict(self):
+        return {n: int(getattr(self, n)) for n, _ in self._fields_}
+
+
+class ServingStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("queued", C.c_uint64),
+                ("admission_waits", C.c_uint64), ("running", C.c_uint32), ("max_running", C.c_uint32),
+                ("arena_bytes", C.c_uint64), ("arena_budget", C.c_uint64)]
+
+    def as_dict(self):
+        return {n: int(getattr(self, n)) for n, _ in self._fields_}
+
+
 class Request(C.Structure):
     _fields_ = [("center", C.c_float * 3), ("side", C.c_float), ("dims", C.c_int), ("precision", C.c_int)]
 
@@ -100,6 +117,10 @@ _SIGS = {
     "adeco_session_latency": ([_vp, C.c_uint64, _i, C.POINTER(_d)], _i),
     "adeco_session_batch_device_ms": ([_vp, C.c_uint64, C.POINTER(C.c_double)], _i),
     "adeco_session_release": ([_vp, C.c_uint64], _i),
+    "adeco_session_get_tuning": ([_vp, C.POINTER(Tuning)], _i),
+    "adeco_session_set_tuning": ([_vp, C.POINTER(Tuning)], _i),
+    "adeco_session_serving_stats": ([_vp, C.POINTER(ServingStats)], _i),
+    "adeco_debug_bounded_wait": ([C.c_uint], _i),
     "adeco_debug_tet_records": ([_vp, _sz, _i, _sz, _sz, _vp, _i, _i, _vp, _vp], _i),
     "adeco_probe_fp32_tflops": ([_i, C.POINTER(_d)], _i),
 }

@@ -223,51 +223,6 @@ ADECO_HD inline float halfspace_cube_vol6(float G0, float nx, float ny, float nz
     return v;
 }
 
-// ---------------------------------------------------- double-float
-// An FP32 pair hi + lo carrying ~44 bits, at FP32 speed: the barycentric
-// shares below need more than FP32, and FP64 runs at a small fraction of the
-// FP32 rate on this GPU.  Sums use Knuth's error-free TwoSum, products the
-// fma-based TwoProd; results are renormalised so |lo| <= ulp(hi) / 2.
-struct F2 {
-    float hi, lo;
-};
-
-ADECO_HD inline F2 f2_two_sum(float a, float b)  // a + b exactly
-{
-    const float s = a + b;
-    const float bb = s - a;
-    return {s, (a - (s - bb)) + (b - bb)};
-}
-
-ADECO_HD inline F2 f2_norm(float a, float b)  // |a| >= |b| or a == 0
-{
-    const float s = a + b;
-    return {s, b - (s - a)};
-}
-
-ADECO_HD inline F2 f2_add(F2 x, F2 y)
-{
-    const F2 s = f2_two_sum(x.hi, y.hi);
-    return f2_norm(s.hi, s.lo + (x.lo + y.lo));
-}
-
-ADECO_HD inline F2 f2_mul(F2 x, F2 y)
-{
-    const float p = x.hi * y.hi;
-    float e = fmaf(x.hi, y.hi, -p);
-    e = fmaf(x.hi, y.lo, e);
-    e = fmaf(x.lo, y.hi, e);
-    return f2_norm(p, e);
-}
-
-ADECO_HD inline F2 f2_mul_f(F2 x, float y)
-{
-    const float p = x.hi * y;
-    float e = fmaf(x.hi, y, -p);
-    e = fmaf(x.lo, y, e);
-    return f2_norm(p, e);
-}
-
 // 2x2 minor a d - b c
 ADECO_HD inline F2 f2_minor(F2 a, F2 d, F2 b, F2 c)
 {

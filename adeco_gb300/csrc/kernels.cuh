@@ -61,6 +61,12 @@ struct DepositParams {
     unsigned long long *route;
     unsigned long long *route_count;
     unsigned long long route_cap;
+    // launch-shape and batching parameters (set by the host, tunable)
+    int per_cta_items;   // items a CTA takes before it exits (0: persistent, until the queue is empty)
+    int share_chunk;     // work sharing: candidate pairs per chunk (zoom grids)
+    int clip_batch;      // partial pairs a warp lists before its engine clips them (64..kQueue)
+    unsigned help_spins; // work sharing: sleeps a helper looks for open slots before leaving
+    unsigned close_spins;  // work sharing: sleeps an owner waits for its helpers (then error bit 3)
 };
 
 enum Stat : int {
@@ -76,19 +82,21 @@ enum Stat : int {
 };
 
 // Per-warp table of up to 32 tets (structure of arrays in shared memory).
+// Two CTAs of 8 warps fill an SM's shared memory to within a few hundred
+// bytes, so the fields are as narrow as their ranges allow.
 struct WarpTets {
     float q[12][32];     // vertices in the tet's anchor-cell frame (cell units), rounded
-    float qlo[12][32];   // rounding remainders: q + qlo carries the FP64 vertex
+    float qlo[12][32];   // rounding remainders: q + qlo carries the vertex to ~44 bits
     float n[4][3][32];   // inward face normals
-    float d[4][32];      // plane offsets: inside <=> n.x - d > 0
+    float d[4][32];      // plane offsets n . (face centroid): inside <=> n.x - d > 0
+    float dlo[4][32];    //   and their remainders (d + dlo: ~44 bits)
     float tol[32];       // FP32 error bound of the plane tests (largest face)
     float bmin[3][32];   // tet AABB in the anchor frame
     float bmax[3][32];
-    double factor6[32];  // mass per unit of 6x clipped volume (FP64)
-    int lo[3][32];       // anchor cell (first candidate cell) in grid indices
-    int ex[3][32];       // candidate extents (cells per axis)
+    float f6[32];        // mass per unit of 6x clipped volume (tet mass / |6V| in cell units)
+    uint16_t lo[3][32];  // anchor cell (first candidate cell) in grid indices (dims <= 4096)
+    uint16_t ex[3][32];  // candidate extents (cells per axis)
     int scan[33];        // exclusive prefix of candidate counts
-    int tetid[32];       // staged cube * 6 + tet of the slot (FP64 route)
 };
 
 // Tets whose conditioning kappa = (longest edge)^3 / |6V| exceeds this take
@@ -97,12 +105,24 @@ struct WarpTets {
 // miss the 1e-5 per-cell bar.  Lattice tets sit near kappa = 5.2.
 constexpr float kKappaFp64 = 32.f;
 
-// Work sharing inside an item: pairs per chunk, and the bounded waits (a
-// helper looking for work gives up; an owner waiting for its helpers sets
-// error bit 8 and goes on).
+// Work sharing inside an item: default pairs per chunk, and the default
+// bounds of its waits (a helper looking for work gives up; an owner waiting
+// for its helpers sets error bit 3 -- the value 8 -- and goes on).
 constexpr int kChunk = 512;
 constexpr unsigned kHelpSpins = 1u << 14;
 constexpr unsigned kCloseSpins = 1u << 26;
+
+// Waits, sleeping `ns` between looks, until *count is 0, at most `limit`
+// looks; false if the limit ran out first.  Every spin-wait of the deposit
+// kernels goes through here, so that none can wait forever.
+__device__ __forceinline__ bool wait_zero_bounded(const int *count, unsigned limit, unsigned ns)
+{
+    for (unsigned spin = 0; *(volatile const int *)count != 0; ++spin) {
+        if (spin >= limit) return false;
+        __nanosleep(ns);
+    }
+    return true;
+}
 
 struct SharedMixed {
     float4 vert[kMaxVerts];
@@ -164,9 +184,9 @@ __device__ __forceinline__ void stage_block(const DepositParams &P, const Item &
         }
         vert[v] = p;
         if (gh) {
-            grid_frame(p.x, __ldg(&gd->gmin_d[0]), __ldg(&gd->scale_d[0]), gh[0][v], gl[0][v]);
-            grid_frame(p.y, __ldg(&gd->gmin_d[1]), __ldg(&gd->scale_d[1]), gh[1][v], gl[1][v]);
-            grid_frame(p.z, __ldg(&gd->gmin_d[2]), __ldg(&gd->scale_d[2]), gh[2][v], gl[2][v]);
+            grid_frame(p.x, __ldg(&gd->gmin[0]), __ldg(&gd->scale_hi[0]), __ldg(&gd->scale_lo[0]), gh[0][v], gl[0][v]);
+            grid_frame(p.y, __ldg(&gd->gmin[1]), __ldg(&gd->scale_hi[1]), __ldg(&gd->scale_lo[1]), gh[1][v], gl[1][v]);
+            grid_frame(p.z, __ldg(&gd->gmin[2]), __ldg(&gd->scale_hi[2]), __ldg(&gd->scale_lo[2]), gh[2][v], gl[2][v]);
         }
     }
 }
@@ -250,7 +270,7 @@ ADECO_HD inline int setup_tet(const float3 vin[4], const float ghin[4][3], const
     for (int a = 0; a < 3; ++a) {
         const float g0 = ghin[0][a], g1 = ghin[1][a], g2 = ghin[2][a], g3 = ghin[3][a];
         const float bmn = fminf(fminf(g0, g1), fminf(g2, g3)), bmx = fmaxf(fmaxf(g0, g1), fmaxf(g2, g3));
-        const float ir = (float)g.inv_rcell[a];
+        const float ir = g.inv_rcell_f[a];
         const float m0 = 4e-7f * (fabsf(bmn) + 2.f), m1 = 4e-7f * (fabsf(bmx) + 2.f);
         const int c0 = max(lo[a], (int)floorf((bmn - 1.f) * ir - m0) + 1);
         const int c1 = min(hi[a], (int)ceilf(bmx * ir + m1) - 1);
@@ -260,17 +280,26 @@ ADECO_HD inline int setup_tet(const float3 vin[4], const float ghin[4][3], const
 #pragma unroll
         for (int q = 0; q < 4; ++q) shift_frame(ghin[ord[q]][a], glin[ord[q]][a], c0, g.drcell[a], qf[q][a], ql[q][a]);
     }
-    // |6 V| in the anchor frame from the FP32 pairs, FP64 (the tet's
-    // signed-volume normaliser)
-    double qd[4][3];
+    // |6 V| in the anchor frame from the FP32 pairs, in double-float (the
+    // tet's volume normaliser): edge vectors from vertex 3, then the triple
+    // product with TwoProd / TwoSum
+    F2 e[3][3];
 #pragma unroll
-    for (int q = 0; q < 4; ++q)
+    for (int q = 0; q < 3; ++q)
 #pragma unroll
-        for (int a = 0; a < 3; ++a) qd[q][a] = (double)qf[q][a] + (double)ql[q][a];
-    const double vq6 = fabs(vol6_fast<double>(qd[0], qd[1], qd[2], qd[3]));
-    const double f6 = g.mass_factor / vq6;
+        for (int a = 0; a < 3; ++a) e[q][a] = f2_add(F2{qf[q][a], ql[q][a]}, F2{-qf[3][a], -ql[3][a]});
+    const F2 cx = f2_add(f2_mul(e[1][1], e[2][2]), f2_neg(f2_mul(e[1][2], e[2][1])));
+    const F2 cy = f2_add(f2_mul(e[1][2], e[2][0]), f2_neg(f2_mul(e[1][0], e[2][2])));
+    const F2 cz = f2_add(f2_mul(e[1][0], e[2][1]), f2_neg(f2_mul(e[1][1], e[2][0])));
+    F2 w6 = f2_add(f2_add(f2_mul(e[0][0], cx), f2_mul(e[0][1], cy)), f2_mul(e[0][2], cz));
+    if (w6.hi < 0.f) w6 = f2_neg(w6);
+    const float vq6 = w6.hi;
+    const float f6 = f2_div_to_f(F2{g.mf_hi, g.mf_lo}, w6);  // mass per unit of 6x volume
     // planes from the FP32 vertices: inward normals (outward ones negated:
-    // faces (0,1,2) (0,2,3) (0,3,1) (1,3,2) with offsets v0 v0 v0 v1)
+    // faces (0,1,2) (0,2,3) (0,3,1) (1,3,2)); each plane's offset is taken
+    // through the face's centroid, in double-float from the vertex pairs, so
+    // that the FP32 rounding of the normal only turns the plane about the
+    // centroid (the one-face closed form relies on it)
     const int fa[4] = {0, 0, 0, 1}, fb[4] = {2, 3, 1, 2}, fc[4] = {1, 2, 3, 3};
     float R = 0.f;
 #pragma unroll
@@ -287,11 +316,21 @@ ADECO_HD inline int setup_tet(const float3 vin[4], const float ghin[4][3], const
         const float e2x = qf[fc[f]][0] - qf[fa[f]][0], e2y = qf[fc[f]][1] - qf[fa[f]][1],
                     e2z = qf[fc[f]][2] - qf[fa[f]][2];
         const float nx = e1y * e2z - e1z * e2y, ny = e1z * e2x - e1x * e2z, nz = e1x * e2y - e1y * e2x;
-        const float dd = nx * qf[fa[f]][0] + ny * qf[fa[f]][1] + nz * qf[fa[f]][2];
+        const float nn[3] = {nx, ny, nz};
+        F2 dd = {0.f, 0.f};  // 3 n . centroid = n . (va + vb + vc)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const F2 sum = f2_add(f2_add(F2{qf[fa[f]][a], ql[fa[f]][a]}, F2{qf[fb[f]][a], ql[fb[f]][a]}),
+                                  F2{qf[fc[f]][a], ql[fc[f]][a]});
+            dd = f2_add(dd, f2_mul_f(sum, nn[a]));
+        }
+        const float d_hi = div_rn(dd.hi, 3.f);
+        const float d_lo = div_rn(fmaf(-d_hi, 3.f, dd.hi) + dd.lo, 3.f);
         W.n[f][0][lane] = nx;
         W.n[f][1][lane] = ny;
         W.n[f][2][lane] = nz;
-        W.d[f][lane] = dd;
+        W.d[f][lane] = d_hi;
+        W.dlo[f][lane] = d_lo;
         const float L1 = fmaxf(fmaxf(fabsf(e1x), fabsf(e1y)), fabsf(e1z));
         const float L2 = fmaxf(fmaxf(fabsf(e2x), fabsf(e2y)), fabsf(e2z));
         // generous bound on the FP32 rounding of n.x - d (|x| <= R + 1)
@@ -309,10 +348,10 @@ ADECO_HD inline int setup_tet(const float3 vin[4], const float ghin[4][3], const
     for (int a = 0; a < 3; ++a) {
         W.bmin[a][lane] = fminf(fminf(qf[0][a], qf[1][a]), fminf(qf[2][a], qf[3][a]));
         W.bmax[a][lane] = fmaxf(fmaxf(qf[0][a], qf[1][a]), fmaxf(qf[2][a], qf[3][a]));
-        W.lo[a][lane] = lo[a];
-        W.ex[a][lane] = hi[a] - lo[a] + 1;
+        W.lo[a][lane] = (uint16_t)lo[a];
+        W.ex[a][lane] = (uint16_t)(hi[a] - lo[a] + 1);
     }
-    W.factor6[lane] = f6;
+    W.f6[lane] = f6;
     // conditioning: longest edge cubed over |6V|, both in cell units
     float L2 = 0.f;
 #pragma unroll
@@ -323,7 +362,7 @@ ADECO_HD inline int setup_tet(const float3 vin[4], const float ghin[4][3], const
             L2 = fmaxf(L2, dx * dx + dy * dy + dz * dz);
         }
     const float Lm = sqrtf(L2);
-    *fp64_route = !(Lm * Lm * Lm <= kKappaFp64 * (float)vq6);
+    *fp64_route = !(Lm * Lm * Lm <= kKappaFp64 * vq6);
     return (hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
 }
 
@@ -536,11 +575,14 @@ ADECO_HD inline int classify_pair(const WarpTets &W, const GridDesc &g, int s, i
 }
 
 // 6x volume of cell (a, b, c) ∩ slot s's tet when the cell straddles only
-// face f.  The face's linear function is taken about the face's centroid
-// (from the FP64 vertices q + qlo, in FP64), so that the FP32 rounding of
-// its normal only turns the plane about the centroid: the volume a slightly
-// turned plane adds on one side of the centroid it removes on the other,
-// and the tet's mass stays conserved over its cells.
+// face f.  The face's linear function G(u) = n . (cell origin + u - centroid)
+// is taken about the face's centroid, so that the FP32 rounding of its normal
+// only turns the plane about the centroid: the volume a slightly turned plane
+// adds on one side of the centroid it removes on the other, and the tet's mass
+// stays conserved over its cells.  Its value at the cell origin, n . origin -
+// (d + dlo), cancels terms as large as the tet is wide in cells: it is formed
+// exactly in double-float (TwoProd of n with the integer cell offsets) and
+// rounded once.
 #ifdef __CUDA_ARCH__
 __device__ __noinline__
 #else
@@ -548,30 +590,43 @@ inline
 #endif
 float halfspace_pair_vol6(const WarpTets &W, const GridDesc &g, int s, int a, int b, int c, int f)
 {
-    // faces (0,2,1) (0,3,2) (0,1,3) (1,2,3): the vertex a face leaves out
-    const int skip = (f == 0) ? 3 : ((f == 1) ? 1 : ((f == 2) ? 2 : 0));
     const int cc[3] = {a, b, c};
-    double G0 = 0.0;
+    F2 G = {-W.d[f][s], -W.dlo[f][s]};
+    float small = 0.f;  // the cells' deviation from unit size: n_x c_x dr_x, tiny
 #pragma unroll
     for (int x = 0; x < 3; ++x) {
-        double sum = 0.0;
-#pragma unroll
-        for (int v = 0; v < 4; ++v)
-            if (v != skip) sum += (double)W.q[3 * v + x][s] + (double)W.qlo[3 * v + x][s];
-        G0 += (double)W.n[f][x][s] * ((double)cc[x] * g.rcell[x] - sum * (1.0 / 3.0));
+        const float nx = W.n[f][x][s], fc = (float)cc[x];
+        G = f2_add(G, f2_two_prod(nx, fc));
+        small = fmaf(nx * fc, g.drcell[x], small);
     }
-    return halfspace_cube_vol6((float)G0, W.n[f][0][s], W.n[f][1][s], W.n[f][2][s]);
+    const float G0 = G.hi + (G.lo + small);
+    return halfspace_cube_vol6(G0, W.n[f][0][s], W.n[f][1][s], W.n[f][2][s]);
 }
 
-// mass (FP64) of one (tet, cell) pair -> 64-bit fixed point, added to the cell
+// Non-negative mass of a pair (FP32, about 1e-7 relative) -> the cell's
+// 64-bit fixed-point accumulator, with integer operations only.
 __device__ __noinline__ void scatter(const DepositParams &P, const GridDesc &g, const WarpTets &W, int s, int a,
-                                        int b, int c, double dm)
+                                     int b, int c, float m)
 {
-    const unsigned long long fx = (unsigned long long)llrint(ldexp(dm, g.shift));
+    const unsigned long long fx = to_fixed(m, g.shift);
     if (fx == 0ull) return;
     const long long i = W.lo[0][s] + a, j = W.lo[1][s] + b, k = W.lo[2][s] + c;
     const long long idx = g.out_offset + i + (long long)g.dims * (j + (long long)g.dims * k);
     atomicAdd(P.out + idx, fx);
+}
+
+// A pair's 6x volume, summed in fixed point 2^kVolShift (0 <= vacc < 2^59),
+// times the tet's mass per unit of 6x volume.  The sum is converted to FP32
+// with one rounding from two exact 24-bit parts (bits 35..58 and 11..34): the
+// fma rounds their exact sum to nearest.  Rounding the upper part alone would
+// drop the lower bits first -- a truncation, a bias of -6e-9 relative that
+// showed in the total mass.  Bits 0..10 (below 3e-14 of a tet's 6x volume)
+// are left out.
+ADECO_HD inline float pair_mass(long long vacc, float f6)
+{
+    const float hi = (float)(int)(vacc >> 35), mid = (float)(int)((vacc >> 11) & 0xffffff);
+    const float v = fmaf(hi, 0x1p35f, mid * 0x1p11f);
+    return v * (f6 * 0x1p-56f);
 }
 
 // Tet of slot s in the frame of its candidate cell (a, b, c), as the clip
@@ -636,8 +691,8 @@ __device__ __forceinline__ void clip_list(const DepositParams &P, const GridDesc
         const int local = e & ((1u << 27) - 1);
         const int ex0 = W.ex[0][s], ex1 = W.ex[1][s];
         const int a = local % ex0, r = local / ex0, b = r % ex1, c = r / ex1;
-        const double dm = ldexp((double)pool.vacc[j], -kVolShift) * W.factor6[s];
-        if (dm > 0.0) scatter(P, g, W, s, a, b, c, dm);
+        const long long v = pool.vacc[j];
+        if (v > 0) scatter(P, g, W, s, a, b, c, pair_mass(v, W.f6[s]));
     }
     __syncwarp();
 }
@@ -671,7 +726,6 @@ __device__ __forceinline__ int group_setup(const DepositParams &P, const SharedM
                 gl[q][a] = S.gl[a][vid[q]];
             }
         cnt = setup_tet(v, gh, gl, g, W, lane, P.error, &route64);
-        W.tetid[lane] = tid;
     }
     st.tets += (cnt > 0);
     route64 = route64 && cnt > 0;
@@ -712,8 +766,10 @@ __device__ __forceinline__ void pair_range(const DepositParams &P, const GridDes
                                            WarpPool &pool, uint32_t *Q, int c0, int c1, int lane, PairStats &st)
 {
     int np = 0;  // partial pairs listed in Q
+    // clip once more than `flush` pairs are listed (then np + 32 <= kQueue)
+    const int flush = min(max(P.clip_batch, 64), kQueue) - 32;
     for (int pb = c0;; pb += 32) {
-        if (np > kQueue - 32 || (pb >= c1 && np)) {
+        if (np > flush || (pb >= c1 && np)) {
             clip_list(P, g, Wc, pool, Q, np, st.fb);
             np = 0;
         }
@@ -737,17 +793,17 @@ __device__ __forceinline__ void pair_range(const DepositParams &P, const GridDes
             if (cls == P_TET_INSIDE) {
                 ++st.in;
                 ++st.bbox;
-                scatter(P, g, Wc, s, a, b, c, (double)g.tet_mass);
+                scatter(P, g, Wc, s, a, b, c, g.tet_mass);
             } else if (cls == P_CELL_INSIDE) {
                 ++st.cin;
                 ++st.bbox;
-                scatter(P, g, Wc, s, a, b, c, 6.0 * Wc.factor6[s]);
+                scatter(P, g, Wc, s, a, b, c, 6.f * Wc.f6[s]);
             } else if (cls == P_PARTIAL) {
                 ++st.part;
                 ++st.bbox;
                 if (cross >= 0) {  // one face cuts the cell: closed form, no clipping
-                    const double dm = (double)halfspace_pair_vol6(Wc, g, s, a, b, c, cross) * Wc.factor6[s];
-                    if (dm > 0.0) scatter(P, g, Wc, s, a, b, c, dm);
+                    const float dm = halfspace_pair_vol6(Wc, g, s, a, b, c, cross) * Wc.f6[s];
+                    if (dm > 0.f) scatter(P, g, Wc, s, a, b, c, dm);
                 } else {
                     part = true;
                     entry = ((uint32_t)s << 27) | (uint32_t)local;
@@ -766,7 +822,7 @@ __device__ __forceinline__ void pair_range(const DepositParams &P, const GridDes
 // counter, so no warp waits for another until the item is done.
 // kShare (zoom batches): a group with more than one chunk of pairs is
 // published in its warp's slot, and warps whose groups are done take chunks
-// of kChunk pairs from open slots instead of waiting for the slowest warp at
+// of P.share_chunk pairs from open slots instead of waiting for the slowest warp at
 // the end of the item.  On fine grids an item holds few tets with thousands
 // of cells each, and one warp carried most of it (zoom batch 8.19 s without,
 // 6.2 s with).  On coarse grids every group is a single chunk: kShare false
@@ -782,12 +838,16 @@ __global__ void __launch_bounds__(kThreads, 2) deposit_mixed_kernel(DepositParam
     uint32_t *Q = S.queue[warp];
     WarpPool &pool = S.pool[warp];
     PairStats st;
+    const int chunk = P.share_chunk > 0 ? P.share_chunk : kChunk;  // pairs per shared chunk (> 0)
     if (kShare && threadIdx.x < kWarps) {
         S.slot_busy[threadIdx.x] = 0;
         S.slot_open[threadIdx.x] = 0;
     }
 
-    for (;;) {
+    for (int taken = 0;; ++taken) {
+        // one-item CTAs (serving): a CTA exits after its items, so that the
+        // CTAs of other requests' launches get SMs as these finish
+        if (P.per_cta_items > 0 && taken >= P.per_cta_items) break;
         if (threadIdx.x == 0) {
             S.item = atomicAdd(P.counter, 1);
             S.n_cubes = 0;
@@ -840,7 +900,7 @@ __global__ void __launch_bounds__(kThreads, 2) deposit_mixed_kernel(DepositParam
                         total = group_setup(P, S, W, g, grp, ntet, vx, vy, cvx, cvy, lane, st, route64, tid);
                         group_route(P, S, item, route64, tid);
                         // a group of one chunk or less is kept private
-                        const bool pub = total > kChunk;
+                        const bool pub = total > chunk;
                         if (lane == 0) {
                             if (pub) {
                                 S.slot_total[warp] = total;
@@ -882,7 +942,7 @@ __global__ void __launch_bounds__(kThreads, 2) deposit_mixed_kernel(DepositParam
                             }
                             h = __shfl_sync(0xffffffffu, h, 0);
                             set = __shfl_sync(0xffffffffu, set, 0);
-                            if (h >= 0 || set >= ngroups || spin > kHelpSpins) break;
+                            if (h >= 0 || set >= ngroups || spin > P.help_spins) break;
                             __nanosleep(256);
                         }
                         if (h < 0) break;
@@ -896,7 +956,7 @@ __global__ void __launch_bounds__(kThreads, 2) deposit_mixed_kernel(DepositParam
                 if (own_next >= 0) {
                     own_next = total;
                 } else {
-                    if (lane == 0) c0 = atomicAdd(&S.slot_next[cur], kChunk);
+                    if (lane == 0) c0 = atomicAdd(&S.slot_next[cur], chunk);
                     c0 = __shfl_sync(0xffffffffu, c0, 0);
                 }
                 if (c0 >= total) {
@@ -907,20 +967,14 @@ __global__ void __launch_bounds__(kThreads, 2) deposit_mixed_kernel(DepositParam
                             // close the slot, then wait for the helpers still reading W
                             *(volatile int *)&S.slot_open[warp] = 0;
                             __threadfence_block();
-                            for (unsigned spin = 0; *(volatile int *)&S.slot_busy[warp] != 0; ++spin) {
-                                if (spin > kCloseSpins) {
-                                    atomicOr(P.error, 8);
-                                    break;
-                                }
-                                __nanosleep(32);
-                            }
+                            if (!wait_zero_bounded(&S.slot_busy[warp], P.close_spins, 32)) atomicOr(P.error, 8);
                         }
                     }
                     __syncwarp();
                     cur = -1;
                     continue;
                 }
-                pair_range(P, g, S.wt[cur], pool, Q, c0, min(total, c0 + kChunk), lane, st);
+                pair_range(P, g, S.wt[cur], pool, Q, c0, min(total, c0 + chunk), lane, st);
             }
         }
         __syncthreads();

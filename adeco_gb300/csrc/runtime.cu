@@ -116,8 +116,15 @@ GridDesc make_grid(const float bbox[6], int dims, double tet_mass, int shift, lo
         g.rcell[a] = g.delta_d[a] * g.scale_d[a];
         g.inv_rcell[a] = 1.0 / g.rcell[a];
         g.drcell[a] = (float)(g.rcell[a] - 1.0);
+        g.inv_rcell_f[a] = (float)g.inv_rcell[a];
     }
     g.tet_mass = (float)tet_mass;
+    for (int a = 0; a < 3; ++a) {
+        g.scale_hi[a] = (float)g.scale_d[a];
+        g.scale_lo[a] = (float)(g.scale_d[a] - (double)g.scale_hi[a]);
+    }
+    g.mf_hi = (float)g.mass_factor;
+    g.mf_lo = (float)(g.mass_factor - (double)g.mf_hi);
     g.dims = dims;
     g.shift = shift;
     g.out_offset = out_offset;
@@ -162,9 +169,28 @@ int mixed_setup(int device, DeviceProps &dp)
     return ADECO_OK;
 }
 
-struct LaunchStats {
-    uint64_t launches = 0;
+// Launch-shape and batching parameters (adeco_tuning), per session.
+struct Tuning {
+    int zoom_tile = 64;                       // cells per tile edge of a zoom grid
+    int share_chunk = kChunk;                 // work sharing: pairs per chunk
+    int clip_batch = kQueue;                  // partial pairs listed per warp before clipping
+    int ctas_per_sm = 0;                      // persistent launches: CTAs per SM (0: occupancy)
+    unsigned long long route_capacity = 0;    // 0: route_capacity(items)
 };
+
+// Deposit parameters with every field that is not a pointer or a count set
+// to its default (or tuned) value.
+DepositParams base_params(const Tuning &t)
+{
+    DepositParams P;
+    std::memset(&P, 0, sizeof P);
+    P.per_cta_items = 0;
+    P.share_chunk = t.share_chunk;
+    P.clip_batch = t.clip_batch;
+    P.help_spins = kHelpSpins;
+    P.close_spins = kCloseSpins;
+    return P;
+}
 
 // Entries of the list of ill-conditioned tets a mixed launch over n_items
 // items may fill (count word + entries; 8 bytes each): a quarter of a tet per
@@ -194,12 +220,13 @@ static int deposit_error(int err, const char *where)
 // launch that deposits the ill-conditioned tets it listed.  share: warps of
 // an item share the pairs of large tet groups (zoom grids, whose cells are
 // much smaller than the tets).
-int launch_mixed(const DeviceProps &dp, DepositParams P, bool share, cudaStream_t st)
+int launch_mixed(const DeviceProps &dp, DepositParams P, bool share, cudaStream_t st, int ctas_per_sm = 0)
 {
     if (P.n_items <= 0) return ADECO_OK;
     CUDA_TRY(cudaMemsetAsync(P.counter, 0, sizeof(int), st));
     CUDA_TRY(cudaMemsetAsync(P.route_count, 0, sizeof(unsigned long long), st));
-    const int grid = std::max(1, std::min(P.n_items, dp.sms * dp.mixed_blocks_per_sm));
+    const int per_sm = ctas_per_sm > 0 ? std::min(ctas_per_sm, dp.mixed_blocks_per_sm) : dp.mixed_blocks_per_sm;
+    const int grid = std::max(1, std::min(P.n_items, dp.sms * per_sm));
     if (share)
         deposit_mixed_kernel<true><<<grid, kThreads, dp.mixed_smem, st>>>(P);
     else
@@ -317,8 +344,7 @@ static int deposit_device_core(int dev, const float *d_pos, size_t patch_offset,
     CUDA_TRY(cudaMemsetAsync(d_counter.p, 0, 2 * sizeof(int), st));
     CUDA_TRY(cudaMemcpyAsync(d_items.p, items.data(), items.size() * sizeof(Item), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(d_grid.p, &g, sizeof g, cudaMemcpyHostToDevice, st));
-    DepositParams P;
-    std::memset(&P, 0, sizeof P);
+    DepositParams P = base_params(Tuning());
     P.items = d_items.p;
     P.n_items = (int)items.size();
     P.src_kind = SRC_PATCH_F3;
@@ -523,11 +549,13 @@ struct adeco_session {
     cudaGraphExec_t graph_exec = nullptr;
     cudaGraph_t graph = nullptr;
     std::mutex mu;
-    // batches (serving)
-    struct Batch;
-    std::map<uint64_t, std::shared_ptr<Batch>> batches;
-    uint64_t next_batch = 1;
+    Tuning tuning;
+    // zoom batches and the serving loop (serving.cuh), created at the first submit
+    struct Server *server = nullptr;
+    std::mutex server_mu;
 };
+
+static void server_destroy(adeco_session *s);
 
 static void session_drop_graph(adeco_session *s)
 {
@@ -773,6 +801,7 @@ extern "C" int adeco_session_destroy(adeco_session *s)
 {
     if (!s) return ADECO_OK;
     cudaSetDevice(s->device);
+    server_destroy(s);
     if (s->stream) cudaStreamSynchronize(s->stream);
     session_drop_graph(s);
     if (s->stream) cudaStreamDestroy(s->stream);
@@ -927,8 +956,7 @@ extern "C" int adeco_session_leaf_meta(adeco_session *s, int leaf_index, uint64_
 
 static DepositParams session_params(adeco_session *s, bool stats)
 {
-    DepositParams P;
-    std::memset(&P, 0, sizeof P);
+    DepositParams P = base_params(s->tuning);
     P.items = s->d_items.p;
     P.n_items = (int)s->leaf_items.size();
     P.src_kind = SRC_LATTICE_F4;
@@ -943,7 +971,8 @@ static DepositParams session_params(adeco_session *s, bool stats)
     P.counter = s->d_counter.p;
     P.error = s->d_counter.p + 1;
     P.stats = stats ? s->d_stats.p : nullptr;
-    set_route(P, s->d_route.p, s->route_cap);
+    set_route(P, s->d_route.p, s->tuning.route_capacity ? std::min(s->tuning.route_capacity, s->route_cap)
+                                                          : s->route_cap);
     return P;
 }
 
@@ -952,7 +981,7 @@ static int enqueue_leaves_mixed(adeco_session *s, bool stats)
 {
     const size_t nv = s->out_values;
     CUDA_TRY(cudaMemsetAsync(s->d_fixed.p, 0, nv * sizeof(unsigned long long), s->stream));
-    int rc = launch_mixed(s->dp, session_params(s, stats), false, s->stream);
+    int rc = launch_mixed(s->dp, session_params(s, stats), false, s->stream, s->tuning.ctas_per_sm);
     if (rc) return rc;
     const long long cells = (long long)s->leaf_dims * s->leaf_dims * s->leaf_dims;
     fixed_to_f64_grids_kernel<<<s->dp.sms * 4, 256, 0, s->stream>>>(s->d_fixed.p, s->d_out.p, s->d_grids.p,
@@ -1000,7 +1029,7 @@ extern "C" int adeco_session_deposit_leaves(adeco_session *s, int precision, dou
     } else {
         CUDA_TRY(cudaMemsetAsync(s->d_fixed.p, 0, s->out_values * sizeof(unsigned long long), s->stream));
         CUDA_TRY(cudaEventRecord(e0, s->stream));
-        rc = launch_mixed(s->dp, session_params(s, collect_stats != 0), false, s->stream);
+        rc = launch_mixed(s->dp, session_params(s, collect_stats != 0), false, s->stream, s->tuning.ctas_per_sm);
         launches = 2;  // the mixed kernel and the ill-conditioned-tet launch
         CUDA_TRY(cudaEventRecord(e1, s->stream));
         const long long cells = (long long)s->leaf_dims * s->leaf_dims * s->leaf_dims;
@@ -1135,274 +1164,35 @@ extern "C" int adeco_debug_tet_records(const float *positions, size_t positions_
     return ADECO_OK;
 }
 
-// ============================================================ zoom batches
-// A batch of zoom requests: each request is a cubic box and a resolution; its
-// work items pair the request grid with every meta-cell whose AABB strictly
-// meets the box.  A batch is one persistent launch on its own stream, so
-// batches submitted while others run overlap on the device.
-struct adeco_session::Batch {
-    std::vector<adeco_request> reqs;
-    std::vector<GridDesc> grids;     // one per tile of each request
-    std::vector<long long> offsets;  // first cell of each request
-    std::vector<int> shifts;         // fixed-point scale of each request
-    size_t cells = 0;
-    cudaStream_t stream = nullptr;
-    cudaEvent_t done = nullptr;
-    cudaEvent_t t0 = nullptr, t1 = nullptr;  // device time of the batch's deposit
-    DevBuf<Item> d_items;
-    DevBuf<GridDesc> d_grids;
-    DevBuf<unsigned long long> d_fixed;
-    DevBuf<int> d_counter;
-    DevBuf<unsigned long long> d_route;
-    std::chrono::steady_clock::time_point t_submit;
-    double latency_ms = -1.0;
-    int n_items = 0;
-    int err = -1;  // the launch's device error flag, read once when a result is first taken
-    ~Batch()
-    {
-        if (done) cudaEventDestroy(done);
-        if (t0) cudaEventDestroy(t0);
-        if (t1) cudaEventDestroy(t1);
-        if (stream) cudaStreamDestroy(stream);
-    }
-};
+// ============================================================ zoom batches and serving
+#include "serving.cuh"
 
-constexpr int kZoomTile = 64;  // cells per tile edge of a zoom grid
-
-static void request_box(const adeco_request &r, float bb[6])
+// ============================================================ bounded waits
+// One warp waits, through wait_zero_bounded (the wait every spin of the
+// deposit kernels uses), on a count that nothing decrements; when the limit
+// runs out it sets error bit 3, as the work-sharing wait does, and returns.
+__global__ void bounded_wait_kernel(int *error, unsigned spins)
 {
-    const float h = 0.5f * r.side;
-    for (int a = 0; a < 3; ++a) {
-        bb[2 * a] = r.center[a] - h;
-        bb[2 * a + 1] = r.center[a] + h;
-    }
+    __shared__ int busy;
+    if (threadIdx.x == 0) busy = 1;
+    __syncwarp();
+    if (threadIdx.x == 0 && !wait_zero_bounded(&busy, spins, 32)) atomicOr(error, 8);
 }
 
-extern "C" int adeco_session_submit(adeco_session *s, const adeco_request *reqs, int n, uint64_t *batch_id)
+extern "C" int adeco_debug_bounded_wait(unsigned spins)
 {
-    if (!s || !reqs || n <= 0 || !batch_id) return fail(ADECO_ERR_ARGUMENT, "bad arguments");
-    for (int i = 0; i < n; ++i) {
-        if (reqs[i].dims < 1 || reqs[i].dims > 1024) return fail(ADECO_ERR_ARGUMENT, "request %d: dims out of [1,1024]", i);
-        if (!(reqs[i].side > 0.f)) return fail(ADECO_ERR_ARGUMENT, "request %d: side must be > 0", i);
-        if (reqs[i].precision != ADECO_PREC_MIXED) return fail(ADECO_ERR_ARGUMENT, "request %d: batches run the mixed path", i);
-    }
-    CUDA_TRY(cudaSetDevice(s->device));
-    auto b = std::make_shared<adeco_session::Batch>();
-    b->t_submit = std::chrono::steady_clock::now();
-    b->reqs.assign(reqs, reqs + n);
-    std::vector<Item> items;
-    std::vector<uint32_t> hits;
-    {
-        std::lock_guard<std::mutex> lk(s->mu);
-        if (!s->meta_index.built) s->meta_index.build(s->meta);
-    }
-    long long off = 0;
-    for (int i = 0; i < n; ++i) {
-        float bb[6];
-        request_box(reqs[i], bb);
-        const int d = reqs[i].dims;
-        const GridDesc g0 = make_grid(bb, d, s->tet_mass, 0, off);
-        // Grids larger than kZoomTile^3 cells are split into tiles, one work
-        // item per (tile, meta-cell): when the cells are much smaller than
-        // the tets, a meta-cell's tets cover very many cells, and one work
-        // item per meta-cell would leave all of that to a single CTA.
-        const int nt = (d + kZoomTile - 1) / kZoomTile;
-        const size_t first_grid = b->grids.size(), first = items.size();
-        for (int tz = 0; tz < nt; ++tz)
-            for (int ty = 0; ty < nt; ++ty)
-                for (int tx = 0; tx < nt; ++tx) {
-                    GridDesc gt = g0;
-                    const int t[3] = {tx, ty, tz};
-                    for (int a = 0; a < 3; ++a) {
-                        gt.tile_lo[a] = t[a] * kZoomTile;
-                        gt.tile_hi[a] = std::min(d, (t[a] + 1) * kZoomTile) - 1;
-                        // the tile's world box widened by a cell, inside the grid box
-                        gt.cull_min[a] = std::max(g0.gmin[a], g0.gmin[a] + (float)(gt.tile_lo[a] - 1) * g0.delta[a]);
-                        gt.cull_max[a] = std::min(g0.gmax[a], g0.gmin[a] + (float)(gt.tile_hi[a] + 2) * g0.delta[a]);
-                    }
-                    const float box6[6] = {gt.cull_min[0], gt.cull_min[1], gt.cull_min[2],
-                                           gt.cull_max[0], gt.cull_max[1], gt.cull_max[2]};
-                    s->meta_index.query(s->meta, box6, hits);
-                    if (hits.empty()) continue;
-                    const int grid_index = (int)b->grids.size();
-                    b->grids.push_back(gt);
-                    for (const uint32_t id : hits) {
-                        int org[3], nv[3];
-                        s->meta.range(id, org, nv);
-                        Item it;
-                        it.base = org[0] + (long long)s->nx * (org[1] + (long long)s->ny * org[2]);
-                        it.grid = grid_index;
-                        it.nv = nv[0] | (nv[1] << 8) | (nv[2] << 16);
-                        items.push_back(it);
-                    }
-                }
-        // fixed-point scale from the tets the request can see (all its tiles)
-        const double tets = 2058.0 * (double)std::max<size_t>(1, items.size() - first);
-        const int shift = choose_shift(tets, s->tet_mass);
-        for (size_t k = first_grid; k < b->grids.size(); ++k) b->grids[k].shift = shift;
-        b->shifts.push_back(shift);
-        b->offsets.push_back(off);
-        off += (long long)d * d * d;
-    }
-    b->cells = (size_t)off;
-    b->n_items = (int)items.size();
-    // admission by free HBM
-    size_t free_b = 0, total_b = 0;
-    CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
-    const double need = (double)b->cells * 8.0 + (double)items.size() * sizeof(Item) + 4096.0;
-    if (need > s->hbm_fraction * (double)free_b)
-        return fail(ADECO_ERR_MEMORY, "batch needs %.0f bytes, admission budget %.0f", need,
-                    s->hbm_fraction * (double)free_b);
-    int rc;
-    const unsigned long long rcap = route_capacity((long long)items.size());
-    if ((rc = b->d_items.reserve(items.size())) || (rc = b->d_grids.reserve(b->grids.size())) ||
-        (rc = b->d_fixed.reserve(b->cells)) || (rc = b->d_counter.reserve(2)) || (rc = b->d_route.reserve(rcap + 1)))
-        return rc;
-    CUDA_TRY(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
-    CUDA_TRY(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming));
-    CUDA_TRY(cudaEventCreate(&b->t0));
-    CUDA_TRY(cudaEventCreate(&b->t1));
-    CUDA_TRY(cudaMemcpyAsync(b->d_items.p, items.data(), items.size() * sizeof(Item), cudaMemcpyHostToDevice, b->stream));
-    CUDA_TRY(cudaMemcpyAsync(b->d_grids.p, b->grids.data(), b->grids.size() * sizeof(GridDesc), cudaMemcpyHostToDevice,
-                             b->stream));
-    CUDA_TRY(cudaMemsetAsync(b->d_fixed.p, 0, b->cells * sizeof(unsigned long long), b->stream));
-    CUDA_TRY(cudaMemsetAsync(b->d_counter.p, 0, 2 * sizeof(int), b->stream));
-    DepositParams P;
-    std::memset(&P, 0, sizeof P);
-    P.items = b->d_items.p;
-    P.n_items = b->n_items;
-    P.src_kind = SRC_LATTICE_F4;
-    P.grids = b->d_grids.p;
-    P.src = s->lattice.p;
-    P.stride_y = s->nx;
-    P.stride_z = (long long)s->nx * s->ny;
-    P.order = s->order;
-    P.out = b->d_fixed.p;
-    P.counter = b->d_counter.p;
-    P.error = b->d_counter.p + 1;
-    set_route(P, b->d_route.p, rcap);
-    CUDA_TRY(cudaEventRecord(b->t0, b->stream));
-    if ((rc = launch_mixed(s->dp, P, true, b->stream))) return rc;
-    CUDA_TRY(cudaEventRecord(b->t1, b->stream));
-    CUDA_TRY(cudaEventRecord(b->done, b->stream));
-    std::lock_guard<std::mutex> lk(s->mu);
-    *batch_id = s->next_batch++;
-    s->batches[*batch_id] = b;
-    return ADECO_OK;
-}
-
-static std::shared_ptr<adeco_session::Batch> find_batch(adeco_session *s, uint64_t id)
-{
-    std::lock_guard<std::mutex> lk(s->mu);
-    auto it = s->batches.find(id);
-    return it == s->batches.end() ? nullptr : it->second;
-}
-
-static void mark_done(adeco_session::Batch &b)
-{
-    if (b.latency_ms < 0)
-        b.latency_ms =
-            std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - b.t_submit).count();
-}
-
-extern "C" int adeco_session_poll(adeco_session *s, uint64_t batch_id, int *done)
-{
-    if (!s || !done) return fail(ADECO_ERR_ARGUMENT, "null argument");
-    auto b = find_batch(s, batch_id);
-    if (!b) return fail(ADECO_ERR_NOT_FOUND, "unknown batch %llu", (unsigned long long)batch_id);
-    const cudaError_t e = cudaEventQuery(b->done);
-    if (e == cudaSuccess) {
-        mark_done(*b);
-        *done = 1;
-        return ADECO_OK;
-    }
-    if (e == cudaErrorNotReady) {
-        *done = 0;
-        return ADECO_OK;
-    }
-    return fail(ADECO_ERR_CUDA, "batch %llu failed: %s", (unsigned long long)batch_id, cudaGetErrorString(e));
-}
-
-extern "C" int adeco_session_wait(adeco_session *s, uint64_t batch_id, double timeout_s)
-{
-    if (!s) return fail(ADECO_ERR_ARGUMENT, "null session");
-    auto b = find_batch(s, batch_id);
-    if (!b) return fail(ADECO_ERR_NOT_FOUND, "unknown batch %llu", (unsigned long long)batch_id);
-    const auto t0 = std::chrono::steady_clock::now();
-    for (;;) {
-        const cudaError_t e = cudaEventQuery(b->done);
-        if (e == cudaSuccess) {
-            mark_done(*b);
-            return ADECO_OK;
-        }
-        if (e != cudaErrorNotReady) return fail(ADECO_ERR_CUDA, "batch failed: %s", cudaGetErrorString(e));
-        if (std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() > timeout_s)
-            return fail(ADECO_ERR_STATE, "timed out after %.1f s waiting for batch %llu", timeout_s,
-                        (unsigned long long)batch_id);
-        std::this_thread::yield();
-    }
-}
-
-extern "C" int adeco_session_result(adeco_session *s, uint64_t batch_id, int index, double *host_out, size_t capacity)
-{
-    if (!s || !host_out) return fail(ADECO_ERR_ARGUMENT, "null argument");
-    auto b = find_batch(s, batch_id);
-    if (!b) return fail(ADECO_ERR_NOT_FOUND, "unknown batch %llu", (unsigned long long)batch_id);
-    if (index < 0 || index >= (int)b->reqs.size()) return fail(ADECO_ERR_ARGUMENT, "request index out of range");
-    int rc = adeco_session_wait(s, batch_id, 3600.0);
+    if (spins > (1u << 26)) return fail(ADECO_ERR_ARGUMENT, "spins %u above 2^26", spins);
+    int dev = 0;
+    int rc = select_device(0, 0, dev);
     if (rc) return rc;
-    if (b->err < 0) {
-        int err = 0;
-        CUDA_TRY(cudaMemcpy(&err, b->d_counter.p + 1, sizeof(int), cudaMemcpyDeviceToHost));
-        b->err = err;
-    }
-    if (b->err) return deposit_error(b->err, "a zoom grid");
-    const size_t n = (size_t)b->reqs[index].dims * b->reqs[index].dims * b->reqs[index].dims;
-    if (capacity < n) return fail(ADECO_ERR_ARGUMENT, "capacity %zu < %zu cells", capacity, n);
-    std::vector<unsigned long long> tmp(n);
-    CUDA_TRY(cudaMemcpy(tmp.data(), b->d_fixed.p + b->offsets[index], n * sizeof(unsigned long long),
-                        cudaMemcpyDeviceToHost));
-    const double scale = std::ldexp(1.0, -b->shifts[index]);
-    for (size_t c = 0; c < n; ++c) host_out[c] = (double)tmp[c] * scale;
-    return ADECO_OK;
-}
-
-extern "C" int adeco_session_latency(adeco_session *s, uint64_t batch_id, int index, double *ms)
-{
-    if (!s || !ms) return fail(ADECO_ERR_ARGUMENT, "null argument");
-    auto b = find_batch(s, batch_id);
-    if (!b) return fail(ADECO_ERR_NOT_FOUND, "unknown batch %llu", (unsigned long long)batch_id);
-    if (index < 0 || index >= (int)b->reqs.size()) return fail(ADECO_ERR_ARGUMENT, "request index out of range");
-    if (b->latency_ms < 0) return fail(ADECO_ERR_STATE, "batch not finished");
-    *ms = b->latency_ms;
-    return ADECO_OK;
-}
-
-extern "C" int adeco_session_batch_device_ms(adeco_session *s, uint64_t batch_id, double *ms)
-{
-    if (!s || !ms) return fail(ADECO_ERR_ARGUMENT, "null argument");
-    auto b = find_batch(s, batch_id);
-    if (!b) return fail(ADECO_ERR_NOT_FOUND, "unknown batch %llu", (unsigned long long)batch_id);
-    int rc = adeco_session_wait(s, batch_id, 3600.0);
-    if (rc) return rc;
-    float f = 0.f;
-    CUDA_TRY(cudaEventElapsedTime(&f, b->t0, b->t1));
-    *ms = f;
-    return ADECO_OK;
-}
-
-extern "C" int adeco_session_release(adeco_session *s, uint64_t batch_id)
-{
-    if (!s) return fail(ADECO_ERR_ARGUMENT, "null session");
-    std::shared_ptr<adeco_session::Batch> b;
-    {
-        std::lock_guard<std::mutex> lk(s->mu);
-        auto it = s->batches.find(batch_id);
-        if (it == s->batches.end()) return fail(ADECO_ERR_NOT_FOUND, "unknown batch");
-        b = it->second;
-        s->batches.erase(it);
-    }
-    if (b->stream) cudaStreamSynchronize(b->stream);
+    DevBuf<int> d_err;
+    if ((rc = d_err.reserve(1))) return rc;
+    CUDA_TRY(cudaMemset(d_err.p, 0, sizeof(int)));
+    bounded_wait_kernel<<<1, 32>>>(d_err.p, spins);
+    CUDA_TRY(cudaGetLastError());
+    int err = 0;
+    CUDA_TRY(cudaMemcpy(&err, d_err.p, sizeof err, cudaMemcpyDeviceToHost));
+    if (err) return deposit_error(err, "the bounded-wait check");
     return ADECO_OK;
 }
 
@@ -1470,7 +1260,7 @@ extern "C" int adeco_probe_fp32_tflops(int device, double *tflops)
 namespace {
 constexpr int kNoAllocMaxItems = 4096;                  // patch sub-blocks of <= 7^3 cubes
 constexpr long long kNoAllocMaxCells = 96LL * 96 * 96;  // grid cells (dims <= 96 for a cube)
-constexpr size_t kNoAllocHeader = 512;                  // counter, error flag, GridDesc
+constexpr size_t kNoAllocHeader = 1024;                 // counter, error flag, GridDesc
 // ill-conditioned tets per call: the allocating path's rule at the item limit,
 // so both paths accept the same calls
 constexpr unsigned long long kNoAllocRouteCap = route_capacity(kNoAllocMaxItems);
@@ -1584,8 +1374,7 @@ extern "C" int adeco_deposit_tets_device_noalloc(const float *d_positions, size_
     noalloc_items_kernel<<<(unsigned)((n_items + 127) / 128), 128, 0, st>>>(items, (long long)patch_offset,
                                                                            (int)n_items, m, nsb);
     CUDA_TRY(cudaGetLastError());
-    DepositParams P;
-    std::memset(&P, 0, sizeof P);
+    DepositParams P = base_params(Tuning());
     P.items = items;
     P.n_items = (int)n_items;
     P.src_kind = SRC_PATCH_F3;

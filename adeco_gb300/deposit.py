@@ -282,6 +282,30 @@ class Session:
     def release(self, batch):
         _raise(self._lib.adeco_session_release(self._h, C.c_uint64(batch)))
 
+    def serving_stats(self):
+        st = L.ServingStats()
+        _raise(self._lib.adeco_session_serving_stats(self._h, C.byref(st)))
+        return st.as_dict()
+
+    # --- launch-shape / batching parameters (adeco_tuning)
+    def get_tuning(self):
+        t = L.Tuning()
+        _raise(self._lib.adeco_session_get_tuning(self._h, C.byref(t)))
+        return t.as_dict()
+
+    def set_tuning(self, **fields):
+        """Change the named adeco_tuning fields (zoom_tile, share_chunk, clip_batch,
+        ctas_per_sm, route_capacity); returns the previous values."""
+        t = L.Tuning()
+        _raise(self._lib.adeco_session_get_tuning(self._h, C.byref(t)))
+        old = t.as_dict()
+        for k, v in fields.items():
+            if k not in old:
+                raise AdRuntimeException(L.ERR_ARGUMENT, f"unknown tuning field {k}")
+            setattr(t, k, int(v))
+        _raise(self._lib.adeco_session_set_tuning(self._h, C.byref(t)))
+        return old
+
 
 def leaf_bbox(node):
     """(xmin,xmax,ymin,ymax,zmin,zmax) of an octree node, as the leaf loop forms it."""

@@ -41,7 +41,7 @@ def zeldovich_lattice(n: int, L: float = 100.0, seed: int = 0, rms_disp: float =
     del amp
     psi = np.empty((n, n, n, 3), dtype=np.float64)
     for a, kv in enumerate((kx[None, None, :], ky[None, :, None], kz[:, None, None])):
-        psi[..., a] = np.fft.irfftn(1j * kv * inv_k2 * dk, s=(n, n, n))
+        psi[..., a] = np.fft.irfftn(1j * kv * inv_k2 * dk, s=(n, n, n), axes=(0, 1, 2))
     del dk
     rms = np.sqrt(np.mean(np.sum(psi ** 2, axis=-1)))
     spacing = L / n
@@ -142,6 +142,37 @@ def periodic_ghost_lattice(pos: np.ndarray, L: float) -> np.ndarray:
     out[:n, :n, n] = pos[:, :, 0] + np.array([L, 0, 0], dtype=pos.dtype)
     out[:n, n, :] = out[:n, 0, :] + np.array([0, L, 0], dtype=pos.dtype)
     out[n, :, :] = out[0, :, :] + np.array([0, 0, L], dtype=pos.dtype)
+    return out
+
+
+def lattice_patches(vertices: np.ndarray, m: int) -> np.ndarray:
+    """Cut an (N+1)^3 vertex lattice (shape (N+1, N+1, N+1, 3), x fastest)
+    into (N/m)^3 patches of (m+1)^3 vertices -- the reference boundary's input
+    layout, neighbouring patches sharing a vertex plane -- flattened, patches
+    x fastest."""
+    n = vertices.shape[0] - 1
+    if n % m:
+        raise ValueError(f"{n} cubes per axis is not a multiple of m = {m}")
+    k = n // m
+    out = np.empty((k, k, k, m + 1, m + 1, m + 1, 3), dtype=vertices.dtype)
+    for pz in range(k):
+        for py in range(k):
+            for px in range(k):
+                out[pz, py, px] = vertices[pz * m:pz * m + m + 1, py * m:py * m + m + 1, px * m:px * m + m + 1]
+    return out.reshape(-1)
+
+
+def image_boxes(bbox, L: float):
+    """The 27 periodic images (shifts by -L, 0, +L per axis) of a grid box
+    (xmin, xmax, ymin, ymax, zmin, zmax): depositing into every image and
+    summing wraps the mass that periodic tets carry across the box faces."""
+    b = np.asarray(bbox, dtype=np.float32)
+    out = []
+    for sz in (-1, 0, 1):
+        for sy in (-1, 0, 1):
+            for sx in (-1, 0, 1):
+                sh = np.array([sx, sx, sy, sy, sz, sz], dtype=np.float32) * np.float32(L)
+                out.append((b + sh).astype(np.float32))
     return out
 
 

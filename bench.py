@@ -45,8 +45,9 @@ INFALL = 0
 MAX_TETS = 64 * 16 ** 3
 MAX_LEVEL = 8
 LEAF = 16
-WORKLOAD = ("octree deposit of a 256^3 Zel'dovich lattice (rms disp 3 spacings, seed 0, L=100): "
-            "depth <= 8, 16^3-cell leaves, refine while tet estimate > 262144 (64 per cell)")
+WORKLOAD = ("octree deposit of a 256^3 Zel'dovich lattice (rms disp 3 spacings, seed 0, L=100; the reference's "
+            "non-periodic cube set, 255^3 cubes = 99,488,250 tets): depth <= 8, 16^3-cell leaves, refine while tet "
+            "estimate > 262144 (64 per cell)")
 ZOOM_COUNT, ZOOM_SEED = 512, 1
 SERVE_SEED = 2
 
@@ -170,9 +171,15 @@ def set_size(n):
 
 def set_workload(name):
     """c2: the benchmark (256^3 octree deposit).  c4: 512^3 lattice with 2000
-    infall regions (seed 4), octree depth <= 12.  zoom and serve run on the c2
-    lattice."""
-    global N_PART, SEED, INFALL, MAX_LEVEL, WORKLOAD
+    infall regions (seed 4), octree depth <= 12.  c1: 64^3 periodic lattice
+    onto a uniform 128^3 grid through the reference boundary.  zoom and serve
+    run on the c2 lattice."""
+    global N_PART, SEED, INFALL, MAX_LEVEL, WORKLOAD, RMS_DISP
+    if name == "c1":
+        N_PART, SEED, RMS_DISP = 64, 0, 0.5
+        WORKLOAD = ("periodic 64^3 Zel'dovich lattice (rms disp 0.5 spacings, seed 0, L=100; 64^3 cubes = 1,572,864 "
+                    "tets from ghost planes shifted by +L, 64 patches of 16^3 cubes) onto a uniform 128^3 grid over "
+                    "the box through the reference boundary; periodic wrap = sum over the box's 27 images")
     if name == "c4":
         N_PART, SEED, INFALL, MAX_LEVEL = 512, 4, 2000, 12
         WORKLOAD = ("octree deposit of a 512^3 Zel'dovich lattice with 2000 infall regions (rms disp 3 spacings, "
@@ -315,6 +322,15 @@ def run_ours(args, rank, ws, local):
     with D.Session(pos, device=local if ws > 1 else args.device) as s:
         info = s.build_octree(MAX_TETS, MAX_LEVEL, leaf_dims=LEAF)
         nleaf = len(info.leaves)
+        out["gpu_tree"] = (info, [s.leaf_meta(q) for q in range(nleaf)])
+        # launch shape and staging depth: picked by the autotuner for this GPU and workload
+        if not args.no_tune:
+            from adeco_gb300 import tune
+            params, tinfo = tune.tune_leaves(s, WORKLOAD, device=local if ws > 1 else args.device,
+                                             force=args.retune)
+            out["tuning"] = {"leaf": params, **{k: v for k, v in tinfo.items() if k != "key"}}
+        else:
+            out["tuning"] = {"leaf": s.get_tuning(), "source": "defaults"}
         # one untimed pass with the pair counters on
         grids, st = s.deposit_leaves(stats=True)
         mixed_total = float(grids.sum())
@@ -360,7 +376,7 @@ def run_ours(args, rank, ws, local):
         out["plain"] = plain
         out["mass"] = {"mixed_total": mixed_total, "tet_count": tets}
         leaf_values = grids.size
-        del grids
+        out["grids"] = grids
         # octree generation: the device builder against the host one (same tree)
         tree_ms = {}
         for builder in ("host", "device"):
@@ -401,8 +417,15 @@ def run_ours(args, rank, ws, local):
     dist.close()
     if rank != 0:
         return 0
-    # roofline of the deposit kernel (FP32-pipe bound; HBM figure beside it)
+    # the oracle's octree (generate_tree restated on the CPU) against the GPU's, node for node
     nodes, off, ids, leaves = cpu_tree(pos, n)
+    g_info, g_metas = out.pop("gpu_tree")
+    tree_same = same_tree(g_info, g_metas, nodes, off, ids, leaves)
+    # per-cell parity of the timed path's grids against the FP64 oracle on a spread sample of leaves
+    oracle_check = None if args.skip_oracle_check else oracle_leaf_check(pos, n, out["grids"], nodes, off, ids,
+                                                                          leaves, args.oracle_leaves)
+    del out["grids"]
+    # roofline of the deposit kernel (FP32-pipe bound; HBM figure beside it)
     flops_per_mc = algorithmic_flops(pos, n, nodes, off, ids, leaves)
     total_mc = int(sum(off[L + 1] - off[L] for L in leaves))
     alg_flops = flops_per_mc * total_mc
@@ -455,6 +478,207 @@ def run_ours(args, rank, ws, local):
         "pair_counts": st,
         "mass": out["mass"],
         "octree_build_ms": out["octree_build_ms"],
+        "tree_equals_oracle": tree_same,
+        "oracle_check": oracle_check,
+        "oracle_sample_max_rel": oracle_check["max_rel_cells_gt_1"] if oracle_check else None,
+        "tuning": out["tuning"],
+    }
+    # serving and zoom legs (one GPU, rank 0): the library's continuous batching
+    if ws == 1 and not args.skip_serve:
+        sv = serve_leg(args, pos)
+        line["serve"] = sv
+        line["serve_p50_ms"], line["serve_p99_ms"] = sv["p50_ms"], sv["p99_ms"]
+    if ws == 1 and not args.skip_zoom:
+        zm = zoom_leg(args, pos)
+        line["zoom"] = zm
+        line["zoom_requests_per_s"] = zm["requests_per_s"]
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def same_tree(info, metas, nodes, off, ids, leaves):
+    """True when the GPU octree equals the oracle's: every node's box, level,
+    parent, first child and estimate, the leaf order, every leaf's meta-cells."""
+    g = info.nodes
+    if len(g) != len(nodes) or not np.array_equal(info.leaves, leaves):
+        return False
+    for f in ("ext", "level", "parent", "first_child", "estimate"):
+        if not np.array_equal(g[f], nodes[f]):
+            return False
+    if not np.array_equal(g["min"], nodes["min"]):
+        return False
+    return all(np.array_equal(m, ids[off[L]:off[L + 1]]) for m, L in zip(metas, leaves))
+
+
+def oracle_leaf_check(pos, n, grids, nodes, off, ids, leaves, count):
+    """The timed path's leaf grids against the FP64 oracle (the reference's
+    deposit_tet_2_grid<double,double> restated) on `count` leaves spread over
+    the leaf order, per cell: relative error on cells above 1 and 1e-2 tet
+    masses, and the 1e-5 relative + 1e-7 tet-mass bar on every cell."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from oracle import oracle as O
+    flat = np.ascontiguousarray(pos.reshape(-1))
+    nl = len(leaves)
+    pick = sorted(set(int(round(k * (nl - 1) / max(1, count - 1))) for k in range(min(count, nl))))
+
+    def leaf_box(L):
+        nd = nodes[L]
+        return np.array([nd["min"][0], nd["min"][0] + nd["ext"], nd["min"][1], nd["min"][1] + nd["ext"],
+                         nd["min"][2], nd["min"][2] + nd["ext"]], np.float32)
+
+    def ref(q):
+        L = leaves[q]
+        return O.deposit_meta(flat, (n, n, n), ids[off[L]:off[L + 1]], leaf_box(L), LEAF, fp64=True)
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:
+        refs = list(ex.map(ref, pick))
+    got = np.concatenate([grids[q].reshape(-1) for q in pick])
+    want = np.concatenate([r.reshape(-1) for r in refs])
+    d = np.abs(got - want)
+    out = {"leaves": len(pick), "of_leaves": nl, "cells": int(want.size), "seconds": time.perf_counter() - t0}
+    for th in (1.0, 1e-2):
+        sel = want > th
+        out[f"max_rel_cells_gt_{th:g}"] = float((d[sel] / want[sel]).max()) if sel.any() else 0.0
+    out["max_abs_tet_masses"] = float(d.max())
+    out["bar_1e-5_rel_plus_1e-7_abs_ok"] = bool(np.all(d <= 1e-5 * want + 1e-7))
+    out["mass_rel_diff"] = float(abs(got.sum() - want.sum()) / want.sum())
+    return out
+
+
+def serve_leg(args, pos):
+    """Poisson stream of 128^3-cell zoom requests against the resident lattice."""
+    from adeco_gb300 import deposit as D
+    from adeco_gb300.synthetic import poisson_requests
+    stream = poisson_requests(args.serve_rate, args.serve_seconds, L=L_BOX, seed=SERVE_SEED,
+                              dims=tuple(args.serve_dims))
+    with D.Session(pos, device=args.device) as s:
+        res = serve_stream(s, stream, args.serve_seconds + args.serve_drain_s)
+    lat = np.sort(np.asarray(res["lat"]))
+    return {"workload": f"Poisson arrivals at {args.serve_rate:g} req/s for {args.serve_seconds:g} s (seed "
+                        f"{SERVE_SEED}): zoom boxes, centre uniform, side log-uniform [0.005L, 0.5L], resolution "
+                        f"from {args.serve_dims}; one batch per request, submitted at its arrival",
+            "p50_ms": float(np.percentile(lat, 50)), "p90_ms": float(np.percentile(lat, 90)),
+            "p99_ms": float(np.percentile(lat, 99)), "max_ms": float(lat[-1]), "requests": int(lat.size),
+            "offered_rate": args.serve_rate, "achieved_rate": lat.size / res["wall"],
+            "unfinished_at_deadline": res["unfinished"], "serving_stats": res["stats"]}
+
+
+def zoom_leg(args, pos):
+    """512 zoom requests (C3) in one batch: autotuned tile / chunk / staging
+    depth on a 64-request sample, then whole batches timed on the device."""
+    from adeco_gb300 import deposit as D
+    from adeco_gb300 import tune
+    from adeco_gb300.synthetic import zoom_requests
+    reqs = zoom_requests(args.zoom_count, L=L_BOX, seed=ZOOM_SEED, dims=tuple(args.zoom_dims))
+    cells = sum(r[2] ** 3 for r in reqs)
+    with D.Session(pos, device=args.device) as s:
+        if args.no_tune:
+            params, tinfo = s.get_tuning(), {"source": "defaults"}
+        else:
+            params, tinfo = tune.tune_zoom(s, reqs[:64], f"{len(reqs)} zoom requests, seed {ZOOM_SEED}",
+                                           device=args.device, force=args.retune)
+        ms = []
+        for k in range(1 + args.zoom_steps):
+            b = s.submit(reqs)
+            t = s.device_ms(b)
+            if k == 0:
+                j = min(range(len(reqs)), key=lambda i: reqs[i][2])
+                b1 = s.submit([reqs[j]])
+                same = bool(np.array_equal(s.result(b1, 0, reqs[j][2]), s.result(b, j, reqs[j][2])))
+                s.release(b1)
+            else:
+                ms.append(t)
+            s.release(b)
+    m = statistics.median(ms)
+    return {"workload": f"{len(reqs)} zoom requests (seed {ZOOM_SEED}): centres uniform, side log-uniform "
+                        f"[0.01L, 0.25L], resolution from {args.zoom_dims}, one batch", "cells": cells,
+            "ms_per_batch": m, "requests_per_s": len(reqs) / (m * 1e-3), "cells_per_s": cells / (m * 1e-3),
+            "steps": args.zoom_steps, "alone_equals_in_batch": same,
+            "tuning": {"zoom": {k: params[k] for k in ("zoom_tile", "share_chunk", "clip_batch")},
+                       **{k: v for k, v in tinfo.items() if k != "key"}}}
+
+
+# --------------------------------------------------------------- C1: the reference boundary
+def run_c1(args, rank, ws, local):
+    """C1: periodic 64^3 lattice onto a uniform 128^3 grid, through the
+    reference boundary (27 image boxes, each call accumulating).  value: the
+    device-pointer entry point with the patches resident; e2e: the reference
+    signature (adeco_deposit_tets_ex, host buffers, FP64 output) per step."""
+    import torch
+
+    from adeco_gb300 import _lib as LB
+    from adeco_gb300.synthetic import image_boxes, lattice_patches, periodic_ghost_lattice, zeldovich_lattice
+    if rank != 0:
+        return 0
+    n, m, dims = N_PART, 16, 128
+    pos = zeldovich_lattice(n, L=L_BOX, seed=SEED, rms_disp=RMS_DISP)
+    patches = lattice_patches(periodic_ghost_lattice(pos, L_BOX), m)
+    boxes = image_boxes(np.array([0, L_BOX, 0, L_BOX, 0, L_BOX], np.float32), L_BOX)
+    tets = 6 * n ** 3
+    lib = LB.load(build_if_missing=True)
+    npatch = patches.size // (3 * (m + 1) ** 3)
+    d_pos = torch.from_numpy(patches).cuda(args.device)
+    d_out = torch.zeros(dims ** 3, dtype=torch.float64, device=f"cuda:{args.device}")
+    st = torch.cuda.current_stream(args.device)
+    sp = C.c_void_p(st.cuda_stream)
+
+    def device_step():
+        d_out.zero_()
+        for b in boxes:
+            LB.check(lib.adeco_deposit_tets_device(C.c_void_p(d_pos.data_ptr()), patches.size, 0, npatch, m,
+                                                   C.c_void_p(b.ctypes.data), dims, C.c_void_p(d_out.data_ptr()),
+                                                   0, 0, 1.0, sp))
+
+    for _ in range(args.warmup):
+        device_step()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    with ClockSampler(args.device) as clk:
+        e0.record(st)
+        for _ in range(args.steps):
+            device_step()
+        e1.record(st)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    total = float(d_out.sum().item())
+    # e2e: host positions, host FP64 grid, through the reference-shaped entry point
+    from adeco_gb300 import deposit as D
+    host = np.zeros(dims ** 3)
+    e2e_t = []
+    for k in range(1 + args.e2e_steps):
+        host[:] = 0.0
+        t0 = time.perf_counter()
+        for b in boxes:
+            D.deposit_tets_ex(patches, m, b, dims, data=host)
+        if k:
+            e2e_t.append(time.perf_counter() - t0)
+    e2e_s = statistics.median(e2e_t)
+    # CPU baseline: the reference algorithm (FP32 oracle) over every image, all host threads
+    cpu = None
+    if not args.skip_cpu:
+        from oracle import oracle as O
+        threads = os.cpu_count() or 1
+        g32 = np.zeros(dims ** 3, np.float32)
+        t0 = time.perf_counter()
+        for b in boxes:
+            O.deposit_patches(patches, m, b, dims, fp64=False, grid=g32, threads=threads)
+        sec = time.perf_counter() - t0
+        cpu = {"value": tets / sec, "unit": "tets/s", "cores": threads, "kind": "port",
+               "sample": f"the whole workload ({npatch} patches x 27 images, {sec:.1f} s on {threads} threads, FP32 "
+                         f"oracle restatement of the reference deposit)"}
+    line = {
+        "metric": "tets/s deposited", "value": tets / (ms * 1e-3), "unit": "tets/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "tets": tets, "grid": f"{dims}^3", "calls_per_step": len(boxes),
+                   "l2": "inputs smaller than L2; the grid (16 MB) stays in L2 between steps"},
+        "e2e": {"value": tets / e2e_s, "unit": "tets/s", "ms_per_step": e2e_s * 1e3,
+                "h2d_bytes_per_step": int(patches.size * 4 * len(boxes)),
+                "d2h_bytes_per_step": int(dims ** 3 * 8 * len(boxes))},
+        "cpu_baseline": cpu, "clocks": clk.summary(),
+        "mass": {"total": total, "tet_count": tets, "rel_diff": abs(total - tets) / tets},
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -508,7 +732,6 @@ def run_zoom(args, rank, ws, local):
 def run_serve(args, rank, ws, local):
     """Poisson stream of zoom requests, one batch per request as it arrives;
     latency = arrival -> results ready on the device (host clock)."""
-    from adeco_gb300 import _lib as LB
     from adeco_gb300 import deposit as D
     from adeco_gb300.synthetic import poisson_requests
     if rank != 0:
@@ -516,38 +739,9 @@ def run_serve(args, rank, ws, local):
     pos = workload_positions()
     stream = poisson_requests(args.serve_rate, args.serve_seconds, L=L_BOX, seed=SERVE_SEED,
                               dims=tuple(args.serve_dims))
-    lat, refused = [], 0
     with D.Session(pos, device=args.device) as s:
-        for _, r in stream[:3]:  # warm-up
-            b = s.submit([r])
-            s.wait(b)
-            s.release(b)
-        pending = {}
-        t_start = time.perf_counter()
-        i = 0
-        while i < len(stream) or pending:
-            now = time.perf_counter() - t_start
-            if now > args.serve_seconds + args.serve_drain_s:
-                break  # overloaded: stop waiting, report what finished and what did not
-            while i < len(stream) and stream[i][0] <= now:
-                try:
-                    pending[s.submit([stream[i][1]])] = stream[i][0]
-                    i += 1
-                except D.AdecoError as e:
-                    if e.code != LB.ERR_MEMORY or not pending:
-                        raise
-                    refused += 1      # admission: no HBM for it now; retry once something finishes
-                    break
-            for b in list(pending):
-                if s.poll(b):
-                    lat.append((time.perf_counter() - t_start - pending.pop(b)) * 1e3)
-                    s.release(b)
-            time.sleep(0.0002)
-        wall = time.perf_counter() - t_start
-        unfinished = len(pending) + (len(stream) - i)
-        for b in list(pending):
-            s.wait(b)
-            s.release(b)
+        res = serve_stream(s, stream, args.serve_seconds + args.serve_drain_s)
+    lat, wall, unfinished, stats = res["lat"], res["wall"], res["unfinished"], res["stats"]
     lat = np.sort(np.asarray(lat))
     line = {
         "metric": "serving latency p50", "value": float(np.percentile(lat, 50)), "unit": "ms", "n_gpus": 1,
@@ -559,10 +753,44 @@ def run_serve(args, rank, ws, local):
         "p50_ms": float(np.percentile(lat, 50)), "p90_ms": float(np.percentile(lat, 90)),
         "p99_ms": float(np.percentile(lat, 99)), "max_ms": float(lat[-1]),
         "requests": len(lat), "offered_rate": args.serve_rate, "achieved_rate": len(lat) / wall,
-        "admission_retries": refused, "unfinished_at_deadline": unfinished,
+        "unfinished_at_deadline": unfinished, "serving_stats": stats,
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def serve_stream(s, stream, deadline_s):
+    """Replays a Poisson stream [(arrival_s, request)] against session `s`, one
+    batch per request submitted at its arrival time; latency = arrival ->
+    results in host memory (the completion time the library stamps).  The
+    library admits and queues; this loop only submits and polls."""
+    for _, r in stream[:3]:  # warm-up: the server's arena, streams and first chunks
+        b = s.submit([r])
+        s.wait(b)
+        s.release(b)
+    lat, pending = [], {}
+    t_start = time.perf_counter()
+    i = 0
+    while i < len(stream) or pending:
+        now = time.perf_counter() - t_start
+        if now > deadline_s:
+            break  # overloaded: stop waiting, report what finished and what did not
+        while i < len(stream) and stream[i][0] <= now:
+            pending[s.submit([stream[i][1]])] = (stream[i][0], time.perf_counter() - t_start)
+            i += 1
+        for b in list(pending):
+            if s.poll(b):
+                arrival, submitted = pending.pop(b)
+                # the library's own submit -> done time, plus the arrival -> submit lag of this loop
+                lat.append(s.latency_ms(b, 0) + (submitted - arrival) * 1e3)
+                s.release(b)
+        time.sleep(0.0002)
+    wall = time.perf_counter() - t_start
+    unfinished = len(pending) + (len(stream) - i)
+    for b in list(pending):
+        s.wait(b)
+        s.release(b)
+    return {"lat": lat, "wall": wall, "unfinished": unfinished, "stats": s.serving_stats()}
 
 
 def main():
@@ -580,13 +808,20 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--n", type=int, default=None, help="lattice size; the benchmark workload is 256")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c4", "zoom", "serve"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c4", "zoom", "serve"])
     ap.add_argument("--zoom-dims", type=int, nargs="+", default=[32, 64, 128, 256])
     ap.add_argument("--zoom-count", type=int, default=ZOOM_COUNT)
-    ap.add_argument("--serve-rate", type=float, default=200.0)
-    ap.add_argument("--serve-seconds", type=float, default=10.0)
-    ap.add_argument("--serve-dims", type=int, nargs="+", default=[32, 64, 128, 256, 512])
+    ap.add_argument("--serve-rate", type=float, default=100.0)
+    ap.add_argument("--serve-seconds", type=float, default=8.0)
+    ap.add_argument("--serve-dims", type=int, nargs="+", default=[128])
     ap.add_argument("--serve-drain-s", type=float, default=30.0)
+    ap.add_argument("--skip-serve", action="store_true", help="default run: no serving leg")
+    ap.add_argument("--skip-zoom", action="store_true", help="default run: no zoom-batch leg")
+    ap.add_argument("--skip-oracle-check", action="store_true")
+    ap.add_argument("--oracle-leaves", type=int, default=48)
+    ap.add_argument("--zoom-steps", type=int, default=2)
+    ap.add_argument("--no-tune", action="store_true", help="library defaults instead of the autotuner")
+    ap.add_argument("--retune", action="store_true", help="search again even when the tuning cache has a result")
     args = ap.parse_args()
     set_workload(args.workload)
     if args.n:
@@ -600,6 +835,8 @@ def main():
         return run_zoom(args, rank, ws, local)
     if args.workload == "serve":
         return run_serve(args, rank, ws, local)
+    if args.workload == "c1":
+        return run_c1(args, rank, ws, local)
     return run_ours(args, rank, ws, local)
 
 

@@ -219,6 +219,20 @@ int adeco_session_leaf_grids_device(adeco_session *s, const double **d_grids, si
  * times; kernel_ms is the mean device time of one replay. */
 int adeco_session_replay_leaves(adeco_session *s, int reps, adeco_timing *timing);
 
+/* Launch-shape and batching parameters of a session's deposits, picked by
+ * the project's autotuner (adeco_gb300/tune.py) or set by hand.  Get them,
+ * change fields, set them back; out-of-range values return ADECO_ERR_ARGUMENT. */
+typedef struct {
+    int zoom_tile;           /* cells per tile edge of zoom grids, 16..256 (default 64)              */
+    int share_chunk;         /* zoom grids: candidate pairs per work-sharing chunk, 64..8192 (512)  */
+    int clip_batch;          /* partial pairs a warp lists before clipping them, 64..128 (128)      */
+    int ctas_per_sm;         /* CTAs per SM of the persistent leaf launch, 1..2 (2)                 */
+    uint64_t route_capacity; /* ill-conditioned tets one launch may list; more set ADECO_ERR_LIMIT
+                                (0: automatic, max(65536, 256 x work items))                         */
+} adeco_tuning;
+int adeco_session_get_tuning(adeco_session *s, adeco_tuning *t);
+int adeco_session_set_tuning(adeco_session *s, const adeco_tuning *t);
+
 /* ------------------------------------------------------------------ */
 /* Zoom requests, batches and the serving loop                          */
 
@@ -229,9 +243,13 @@ typedef struct {
     int precision;          /* adeco_precision */
 } adeco_request;
 
-/* Queue requests; returns a batch id.  Work is admitted by free HBM and
- * launched as slots free up; requests submitted while others run overlap
- * with them on the device. */
+/* Queue a batch of requests; returns its id at once.  Continuous batching:
+ * a batch is admitted as soon as device memory (a session arena within
+ * hbm_fraction of the HBM free at the first submit) and a stream are free,
+ * and runs concurrently with the batches already on the GPU, its CTAs taking
+ * SMs as theirs finish (cheap batches on higher-priority streams).  Batches
+ * that do not fit yet wait inside the library.  ADECO_ERR_MEMORY only when
+ * the batch alone exceeds the admission budget. */
 int adeco_session_submit(adeco_session *s, const adeco_request *reqs, int n, uint64_t *batch_id);
 /* done = 1 when every request of the batch has finished. */
 int adeco_session_poll(adeco_session *s, uint64_t batch_id, int *done);
@@ -242,7 +260,21 @@ int adeco_session_result(adeco_session *s, uint64_t batch_id, int index, double 
 int adeco_session_latency(adeco_session *s, uint64_t batch_id, int index, double *ms);
 /* device time of the batch's deposit launch (CUDA events on its stream), milliseconds; waits for the batch */
 int adeco_session_batch_device_ms(adeco_session *s, uint64_t batch_id, double *ms);
+/* Frees the batch's results (host staging), waiting on the host for the
+ * batch to finish if it has not; no device-wide synchronisation. */
 int adeco_session_release(adeco_session *s, uint64_t batch_id);
+
+typedef struct {
+    uint64_t submitted;      /* batches submitted                                          */
+    uint64_t completed;      /* batches finished                                           */
+    uint64_t queued;         /* batches waiting for memory or a stream now                 */
+    uint64_t admission_waits;/* admissions that found no memory or stream free             */
+    uint32_t running;        /* batches on the GPU now                                     */
+    uint32_t max_running;    /* most batches on the GPU at once                            */
+    uint64_t arena_bytes;    /* device memory held by the serving arena                    */
+    uint64_t arena_budget;   /* its admission budget                                       */
+} adeco_serving_stats;
+int adeco_session_serving_stats(adeco_session *s, adeco_serving_stats *st);
 
 /* ------------------------------------------------------------------ */
 /* Parity diagnostics (same device functions as the deposit kernels)    */
@@ -255,6 +287,13 @@ int adeco_session_release(adeco_session *s, uint64_t batch_id);
 int adeco_debug_tet_records(const float *positions, size_t positions_size, int meta_cells_per_patch,
                             size_t cube_begin, size_t cube_end, const float bbox[6], int dims, int tet_order,
                             int32_t *records, uint32_t *cand);
+
+/* The bounded wait every spin-wait of the deposit kernels uses, run on a
+ * count that nothing decrements, for at most `spins` sleeps of 32 ns: the
+ * failure path of a wait that runs out, exercised without a fault.  Returns
+ * ADECO_ERR_CUDA with the deposit's "timed out" message (device error bit 3)
+ * when the wait ran out, as it must. */
+int adeco_debug_bounded_wait(unsigned spins);
 
 /* Measured FP32 FMA throughput of `device` (TFLOP/s, 2 flops per FMA): the
  * peak the deposit kernels' roofline fraction is stated against. */

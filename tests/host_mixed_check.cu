@@ -34,12 +34,19 @@ static GridDesc grid(const float bbox[6], int dims)
         g.rcell[a] = g.delta_d[a] * g.scale_d[a];
         g.inv_rcell[a] = 1.0 / g.rcell[a];
         g.drcell[a] = (float)(g.rcell[a] - 1.0);
+        g.inv_rcell_f[a] = (float)g.inv_rcell[a];
         g.tile_lo[a] = 0;
         g.tile_hi[a] = dims - 1;
         g.cull_min[a] = g.gmin[a];
         g.cull_max[a] = g.gmax[a];
     }
     g.tet_mass = 1.f;
+    for (int a = 0; a < 3; ++a) {
+        g.scale_hi[a] = (float)g.scale_d[a];
+        g.scale_lo[a] = (float)(g.scale_d[a] - (double)g.scale_hi[a]);
+    }
+    g.mf_hi = (float)g.mass_factor;
+    g.mf_lo = (float)(g.mass_factor - (double)g.mf_hi);
     g.dims = dims;
     return g;
 }
@@ -71,9 +78,9 @@ int main()
             for (int q = 0; q < 4; ++q) v[q] = corner[tet_conn(t, q)];
             float gh[4][3], gl[4][3];
             for (int q = 0; q < 4; ++q) {
-                grid_frame(v[q].x, g.gmin_d[0], g.scale_d[0], gh[q][0], gl[q][0]);
-                grid_frame(v[q].y, g.gmin_d[1], g.scale_d[1], gh[q][1], gl[q][1]);
-                grid_frame(v[q].z, g.gmin_d[2], g.scale_d[2], gh[q][2], gl[q][2]);
+                grid_frame(v[q].x, g.gmin[0], g.scale_hi[0], g.scale_lo[0], gh[q][0], gl[q][0]);
+                grid_frame(v[q].y, g.gmin[1], g.scale_hi[1], g.scale_lo[1], gh[q][1], gl[q][1]);
+                grid_frame(v[q].z, g.gmin[2], g.scale_hi[2], g.scale_lo[2], gh[q][2], gl[q][2]);
             }
             bool r64 = false;
             int err = 0;
@@ -101,16 +108,18 @@ int main()
                         if (cls == P_TET_INSIDE) {
                             dm = 1.0;
                         } else if (cls == P_CELL_INSIDE) {
-                            dm = 6.0 * W.factor6[0];
+                            dm = (double)(6.f * W.f6[0]);
                         } else if (cls == P_PARTIAL) {
+                            // the GPU's FP32 pair masses (then converted to fixed point exactly)
                             if (cross >= 0) {
-                                dm = (double)halfspace_pair_vol6(W, g, 0, a, b, c, cross) * W.factor6[0];
+                                dm = (double)(halfspace_pair_vol6(W, g, 0, a, b, c, cross) * W.f6[0]);
                                 path = 1;
                             } else {
                                 path = 2;
                                 float p[12];
                                 piece_coords(W, g, 0, a, b, c, p);
-                                dm = std::ldexp((double)clip_piece_serial(p, 0), -kVolShift) * W.factor6[0];
+                                const long long v = clip_piece_serial(p, 0);
+                                dm = v > 0 ? (double)pair_mass(v, W.f6[0]) : 0.0;
                                 ++partial;
                             }
                         }

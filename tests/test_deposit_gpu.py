@@ -220,6 +220,31 @@ def test_clustered_leaves_vs_oracle_fp64(adeco, oracle):
         check_cells(grids[q], r, n_tets=2058 * len(metas[q]))
 
 
+def test_c1_periodic_uniform_grid_vs_oracle_fp64(adeco, oracle):
+    """C1 at full size through the reference boundary: a periodic 64^3
+    Zel'dovich lattice (rms 0.5 spacings, seed 0, L = 100) as 64^3 cubes =
+    1,572,864 tets -- ghost vertex planes shifted by +L, cut into 64 patches
+    of 16^3 cubes -- deposited onto a uniform 128^3 grid over the box; the
+    periodic wrap is the sum over the box's 27 images (each call accumulates,
+    as the reference's deposit_tets does).  Every cell against the FP64
+    oracle (the same image sum) at 1e-5 relative + 1e-7 tet masses; the total
+    is the tet count to 1e-9."""
+    from adeco_gb300.synthetic import image_boxes, lattice_patches, periodic_ghost_lattice, zeldovich_lattice
+    n, L, m, dims = 64, 100.0, 16, 128
+    pos = zeldovich_lattice(n, L=L, seed=0, rms_disp=0.5)
+    patches = lattice_patches(periodic_ghost_lattice(pos, L), m)
+    box = np.array([0, L, 0, L, 0, L], np.float32)
+    got = np.zeros(dims ** 3)
+    ref = np.zeros(dims ** 3)
+    for b in image_boxes(box, L):
+        adeco.deposit_tets_ex(patches, m, b, dims, data=got)
+        oracle.deposit_patches(patches, m, b, dims, fp64=True, grid=ref, threads=os.cpu_count() or 1)
+    tets = 6 * n ** 3
+    assert abs(ref.sum() - tets) <= 1e-9 * tets
+    check_cells(got, ref, n_tets=tets)
+    assert abs(got.sum() - tets) <= 1e-9 * tets, got.sum() - tets
+
+
 def _tree(s, builder, max_tets, max_level, box6=None, roi6=None):
     info = s.build_octree(max_tets, max_level, leaf_dims=8, box6=box6, roi6=roi6, builder=builder)
     return info.nodes, info.leaves, [s.leaf_meta(q) for q in range(len(info.leaves))]
