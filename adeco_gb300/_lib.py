@@ -62,7 +62,7 @@ class Timing(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("zoom_tile", C.c_int), ("share_chunk", C.c_int), ("clip_batch", C.c_int), ("ctas_per_sm", C.c_int),
-                ("route_capacity", C.c_uint64)]
+                ("route_capacity", C.c_uint64), ("item_pairs", C.c_uint32)]
 
     def as_dict(self):
         return {n: int(getattr(self, n)) for n, _ in self._fields_}

@@ -28,27 +28,24 @@ namespace adeco {
 // inside-first even permutation (4 x 2 bits) and inside count per side mask
 #define ADECO_SPLIT_PERM {228, 228, 177, 228, 210, 210, 201, 228, 99, 156, 135, 177, 78, 120, 54, 228}
 #define ADECO_SPLIT_KIN {0, 1, 1, 2, 1, 2, 2, 3, 1, 2, 2, 3, 2, 3, 3, 4}
-#ifdef __CUDACC__
-__constant__ uint8_t c_split_perm[16] = ADECO_SPLIT_PERM;
-__constant__ int8_t c_split_kin[16] = ADECO_SPLIT_KIN;
-#endif
 static const uint8_t h_split_perm[16] = ADECO_SPLIT_PERM;
 static const int8_t h_split_kin[16] = ADECO_SPLIT_KIN;
 
+// The tables are read with lane-dependent masks, which a constant-memory load
+// serialises per distinct address; the entries are therefore taken from two
+// 64-bit immediates (the permutation, a byte per mask) and from the popcount
+// (the inside count) -- the same values as ADECO_SPLIT_PERM / ADECO_SPLIT_KIN.
 ADECO_HD inline int split_perm(int m)
 {
-#ifdef __CUDA_ARCH__
-    return c_split_perm[m];
-#else
-    return h_split_perm[m];
-#endif
+    const unsigned long long w = (m & 8) ? 0xe436784eb1879c63ull : 0xe4c9d2d2e4b1e4e4ull;
+    return (int)((w >> ((m & 7) * 8)) & 0xffu);
 }
 ADECO_HD inline int split_kin(int m)
 {
 #ifdef __CUDA_ARCH__
-    return c_split_kin[m];
+    return __popc((unsigned)m);
 #else
-    return h_split_kin[m];
+    return __builtin_popcount((unsigned)m);
 #endif
 }
 

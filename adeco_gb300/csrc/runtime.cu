@@ -176,6 +176,7 @@ struct Tuning {
     int clip_batch = kQueue;                  // partial pairs listed per warp before clipping
     int ctas_per_sm = 0;                      // persistent launches: CTAs per SM (0: occupancy)
     unsigned long long route_capacity = 0;    // 0: route_capacity(items)
+    unsigned item_pairs = 1u << 18;           // zoom grids: expected candidate pairs per work item
 };
 
 // Deposit parameters with every field that is not a pointer or a count set
@@ -320,6 +321,60 @@ int validate_boundary(size_t patch_offset, size_t num_patches, const float *posi
 }  // namespace
 
 // ============================================================ boundary
+// Per-thread workspace of the boundary entry points.  The reference's
+// deposit_tets is called from several pthreads at once, one grid each
+// (src/AdDynamicLoadBalancing.h:200-205), and allocates and frees its device
+// memory and stream on every call (src/AdDeposit2Grid.cu:353-394, 527-534);
+// here each thread's buffers grow to its largest call and are kept, so a
+// repeated call makes no cudaMalloc, cudaFree (which synchronises the device)
+// or stream creation.  Freed when the thread exits.
+namespace {
+struct BoundaryWork {
+    int dev = -1;
+    cudaStream_t stream = nullptr;  // the reference-signature calls' stream
+    DevBuf<Item> items;
+    DevBuf<GridDesc> grid;
+    DevBuf<int> counter;
+    DevBuf<long long> cube_off;
+    DevBuf<unsigned long long> route, fixed;
+    DevBuf<double> f64;
+    DevBuf<float> pos;
+    double *pinned = nullptr;  // D2H staging of the grid
+    size_t pinned_n = 0;
+    ~BoundaryWork() { drop(); }
+    void drop()
+    {
+        items.release(); grid.release(); counter.release(); cube_off.release();
+        route.release(); fixed.release(); f64.release(); pos.release();
+        if (pinned) cudaFreeHost(pinned);
+        pinned = nullptr;
+        pinned_n = 0;
+        if (stream) cudaStreamDestroy(stream);
+        stream = nullptr;
+    }
+    // the current device's workspace (a thread that moves to another device starts afresh)
+    int bind(int device)
+    {
+        if (dev == device) return ADECO_OK;
+        drop();
+        dev = device;
+        CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        return ADECO_OK;
+    }
+    int staging(size_t n)
+    {
+        if (n <= pinned_n) return ADECO_OK;
+        if (pinned) cudaFreeHost(pinned);
+        pinned = nullptr;
+        pinned_n = 0;
+        CUDA_TRY(cudaHostAlloc((void **)&pinned, n * sizeof(double), cudaHostAllocDefault));
+        pinned_n = n;
+        return ADECO_OK;
+    }
+};
+thread_local BoundaryWork t_work;
+}  // namespace
+
 // Deposit patches [patch_offset, +num_patches) of device-resident patch data
 // into d_fixed (mixed, fixed point 2^shift) or d_f64 (plain FP64).
 static int deposit_device_core(int dev, const float *d_pos, size_t patch_offset, size_t num_patches, int m,
@@ -333,11 +388,12 @@ static int deposit_device_core(int dev, const float *d_pos, size_t patch_offset,
     std::vector<long long> cube_off;
     patch_items(patch_offset, num_patches, m, 0, items, precision == ADECO_PREC_FP64 ? &cube_off : nullptr);
     GridDesc g = make_grid(bbox, dims, tet_mass, shift, 0);
-    DevBuf<Item> d_items;
-    DevBuf<GridDesc> d_grid;
-    DevBuf<int> d_counter;
-    DevBuf<long long> d_cube_off;
-    DevBuf<unsigned long long> d_route;
+    if ((rc = t_work.bind(dev))) return rc;
+    DevBuf<Item> &d_items = t_work.items;
+    DevBuf<GridDesc> &d_grid = t_work.grid;
+    DevBuf<int> &d_counter = t_work.counter;
+    DevBuf<long long> &d_cube_off = t_work.cube_off;
+    DevBuf<unsigned long long> &d_route = t_work.route;
     const unsigned long long rcap = route_capacity((long long)items.size());
     if ((rc = d_items.reserve(items.size())) || (rc = d_grid.reserve(1)) || (rc = d_counter.reserve(2))) return rc;
     if (precision != ADECO_PREC_FP64 && (rc = d_route.reserve(rcap + 1))) return rc;
@@ -405,11 +461,11 @@ extern "C" int adeco_deposit_tets_ex(const adeco_deposit_args *a)
     size_t per_pass = (size_t)((budget - (double)grid_bytes) / (double)patch_bytes);
     per_pass = std::max<size_t>(1, std::min(per_pass, a->num_patches));
 
-    cudaStream_t st;
-    CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-    DevBuf<float> d_pos;
-    DevBuf<unsigned long long> d_fixed;
-    DevBuf<double> d_f64;
+    if ((rc = t_work.bind(dev))) return rc;
+    cudaStream_t st = t_work.stream;
+    DevBuf<float> &d_pos = t_work.pos;
+    DevBuf<unsigned long long> &d_fixed = t_work.fixed;
+    DevBuf<double> &d_f64 = t_work.f64;
     rc = d_pos.reserve(per_pass * fpp);
     if (!rc) rc = (a->precision == ADECO_PREC_FP64) ? d_f64.reserve(ncell) : d_fixed.reserve(ncell);
     if (!rc && a->precision == ADECO_PREC_FP64) {
@@ -441,9 +497,10 @@ extern "C" int adeco_deposit_tets_ex(const adeco_deposit_args *a)
                 fixed_to_f64_kernel<<<blocks, 256, 0, st>>>(d_fixed.p, d_f64.p, (long long)ncell,
                                                             std::ldexp(1.0, -call_shift));
         }
+        if (!rc) rc = t_work.staging(ncell);
         if (!rc) {
-            std::vector<double> host(ncell);
-            if (cudaMemcpyAsync(host.data(), d_f64.p, ncell * sizeof(double), cudaMemcpyDeviceToHost, st) !=
+            const double *host = t_work.pinned;
+            if (cudaMemcpyAsync(t_work.pinned, d_f64.p, ncell * sizeof(double), cudaMemcpyDeviceToHost, st) !=
                     cudaSuccess ||
                 cudaStreamSynchronize(st) != cudaSuccess) {
                 rc = fail(ADECO_ERR_CUDA, "D2H grid: %s", cudaGetErrorString(cudaGetLastError()));
@@ -457,7 +514,6 @@ extern "C" int adeco_deposit_tets_ex(const adeco_deposit_args *a)
         }
     }
     cudaStreamSynchronize(st);
-    cudaStreamDestroy(st);
     return rc;
 }
 
@@ -500,7 +556,8 @@ extern "C" int adeco_deposit_tets_device(const float *d_positions, size_t positi
         return deposit_device_core(dev, d_positions, patch_offset, num_patches, m, bbox, dims, precision, tet_order,
                                    tet_mass, nullptr, d_out, shift, st);
     }
-    DevBuf<unsigned long long> d_fixed;
+    if ((rc = t_work.bind(dev))) return rc;
+    DevBuf<unsigned long long> &d_fixed = t_work.fixed;
     if ((rc = d_fixed.reserve(ncell))) return rc;
     CUDA_TRY(cudaMemsetAsync(d_fixed.p, 0, ncell * sizeof(unsigned long long), st));
     rc = deposit_device_core(dev, d_positions, patch_offset, num_patches, m, bbox, dims, precision, tet_order,

@@ -465,6 +465,24 @@ static int server_get(adeco_session *s, Server *&out)
     return ADECO_OK;
 }
 
+// Tile edge of a request grid of d cells per axis whose tets are r cells
+// wide (lattice spacing over cell size): the tuned edge `tile`, halved down
+// to 8 while one (tile, meta-cell) item is expected to hold more than
+// `item_pairs` candidate pairs -- the meta-cell's tets that reach a tile of
+// T cells, 6 (T/r + 1)^3 of at most 2058, each meeting min(T, r + 1)^3 of its
+// cells.  On fine grids an item of a 64^3 tile held ~1e7 pairs: one CTA
+// carried it for tens of milliseconds while the rest of the GPU idled.
+static int request_tile(int tile, double item_pairs, int d, double r)
+{
+    int T = std::max(1, std::min(tile, d));
+    auto pairs = [r](int t) {
+        const double tets = std::min(2058.0, 6.0 * std::pow((double)t / r + 1.0, 3.0));
+        return tets * std::pow(std::min((double)t, r + 1.0), 3.0);
+    };
+    while (T > 8 && pairs(T) > item_pairs) T = (T + 1) / 2;
+    return T;
+}
+
 static void request_box(const adeco_request &r, float bb[6])
 {
     const float h = 0.5f * r.side;
@@ -507,6 +525,7 @@ extern "C" int adeco_session_get_tuning(adeco_session *s, adeco_tuning *t)
     t->clip_batch = s->tuning.clip_batch;
     t->ctas_per_sm = s->tuning.ctas_per_sm > 0 ? s->tuning.ctas_per_sm : s->dp.mixed_blocks_per_sm;
     t->route_capacity = s->tuning.route_capacity;
+    t->item_pairs = s->tuning.item_pairs;
     return ADECO_OK;
 }
 
@@ -519,6 +538,8 @@ extern "C" int adeco_session_set_tuning(adeco_session *s, const adeco_tuning *t)
     if (t->clip_batch < 64 || t->clip_batch > kQueue)
         return fail(ADECO_ERR_ARGUMENT, "clip_batch %d out of [64,%d]", t->clip_batch, kQueue);
     if (t->ctas_per_sm < 1 || t->ctas_per_sm > 2) return fail(ADECO_ERR_ARGUMENT, "ctas_per_sm %d out of [1,2]", t->ctas_per_sm);
+    if (t->item_pairs < 4096 || t->item_pairs > (1u << 26))
+        return fail(ADECO_ERR_ARGUMENT, "item_pairs %u out of [4096,2^26]", t->item_pairs);
     std::lock_guard<std::mutex> lk(s->mu);
     session_drop_graph(s);  // a captured leaf replay holds the old parameters
     s->tuning.zoom_tile = t->zoom_tile;
@@ -526,6 +547,7 @@ extern "C" int adeco_session_set_tuning(adeco_session *s, const adeco_tuning *t)
     s->tuning.clip_batch = t->clip_batch;
     s->tuning.ctas_per_sm = t->ctas_per_sm;
     s->tuning.route_capacity = t->route_capacity;
+    s->tuning.item_pairs = t->item_pairs;
     return ADECO_OK;
 }
 
@@ -547,10 +569,12 @@ extern "C" int adeco_session_submit(adeco_session *s, const adeco_request *reqs,
     j.t_submit = std::chrono::steady_clock::now();
     j.reqs.assign(reqs, reqs + n);
     int tile;
+    double item_pairs;
     {
         std::lock_guard<std::mutex> lk(s->mu);
         if (!s->meta_index.built) s->meta_index.build(s->meta);
         tile = s->tuning.zoom_tile;
+        item_pairs = (double)s->tuning.item_pairs;
     }
     std::vector<uint32_t> hits;
     long long off = 0;
@@ -559,11 +583,13 @@ extern "C" int adeco_session_submit(adeco_session *s, const adeco_request *reqs,
         request_box(reqs[i], bb);
         const int d = reqs[i].dims;
         const GridDesc g0 = make_grid(bb, d, s->tet_mass, 0, off);
-        // Grids larger than tile^3 cells are split into tiles, one work item
-        // per (tile, meta-cell): when the cells are much smaller than the
-        // tets, a meta-cell's tets cover very many cells, and one item per
-        // meta-cell would leave all of that to a single CTA.
-        const int nt = (d + tile - 1) / tile;
+        // Grids are split into tiles, one work item per (tile, meta-cell):
+        // when the cells are much smaller than the tets, a meta-cell's tets
+        // cover very many cells, and one item per meta-cell would leave all
+        // of that to a single CTA.  The tile edge is the tuned one, halved
+        // while an item's expected candidate pairs exceed item_pairs.
+        const int tile_d = request_tile(tile, item_pairs, d, S->spacing / ((double)reqs[i].side / d));
+        const int nt = (d + tile_d - 1) / tile_d;
         const size_t first_grid = j.grids.size(), first = j.items.size();
         for (int tz = 0; tz < nt; ++tz)
             for (int ty = 0; ty < nt; ++ty)
@@ -571,8 +597,8 @@ extern "C" int adeco_session_submit(adeco_session *s, const adeco_request *reqs,
                     GridDesc gt = g0;
                     const int t[3] = {tx, ty, tz};
                     for (int a = 0; a < 3; ++a) {
-                        gt.tile_lo[a] = t[a] * tile;
-                        gt.tile_hi[a] = std::min(d, (t[a] + 1) * tile) - 1;
+                        gt.tile_lo[a] = t[a] * tile_d;
+                        gt.tile_hi[a] = std::min(d, (t[a] + 1) * tile_d) - 1;
                         // the tile's world box widened by a cell, inside the grid box
                         gt.cull_min[a] = std::max(g0.gmin[a], g0.gmin[a] + (float)(gt.tile_lo[a] - 1) * g0.delta[a]);
                         gt.cull_max[a] = std::min(g0.gmax[a], g0.gmin[a] + (float)(gt.tile_hi[a] + 2) * g0.delta[a]);

@@ -13,7 +13,9 @@ the per-cell bar):
 * ``clip_batch``  -- the staging depth of the clip engine: partial pairs a
   warp lists before it clips them together (deeper lists keep more lanes
   busy, shallower ones clip sooner);
-* ``ctas_per_sm`` -- CTAs per SM of the persistent leaf launch.
+* ``ctas_per_sm`` -- CTAs per SM of the persistent leaf launch;
+* ``item_pairs``  -- the expected candidate pairs above which a zoom
+  request's tile edge is halved (fine grids: smaller items, shorter tails).
 
 The number of tets a warp sets up at once is the warp width (32, one per
 lane); it is not a parameter.  The reference has no tuner: its launch shape
@@ -37,10 +39,10 @@ SPACES = {
     # octree leaf blocks (coarse grids: a tet meets a few cells)
     "leaf": {"clip_batch": [64, 96, 128], "ctas_per_sm": [1, 2]},
     # zoom grids (fine grids: cells much smaller than tets)
-    "zoom": {"zoom_tile": [32, 48, 64, 96, 128], "share_chunk": [256, 512, 1024, 2048],
-             "clip_batch": [64, 96, 128]},
+    "zoom": {"zoom_tile": [32, 48, 64, 96, 128], "item_pairs": [1 << 16, 1 << 17, 1 << 18, 1 << 20],
+             "share_chunk": [256, 512, 1024, 2048], "clip_batch": [64, 96, 128]},
 }
-DEFAULTS = {"zoom_tile": 64, "share_chunk": 512, "clip_batch": 128, "ctas_per_sm": 2}
+DEFAULTS = {"zoom_tile": 64, "share_chunk": 512, "clip_batch": 128, "ctas_per_sm": 2, "item_pairs": 1 << 18}
 
 
 def search(space, measure, start=None, max_passes=2, log=None):

@@ -596,7 +596,7 @@ def zoom_leg(args, pos):
                         f"[0.01L, 0.25L], resolution from {args.zoom_dims}, one batch", "cells": cells,
             "ms_per_batch": m, "requests_per_s": len(reqs) / (m * 1e-3), "cells_per_s": cells / (m * 1e-3),
             "steps": args.zoom_steps, "alone_equals_in_batch": same,
-            "tuning": {"zoom": {k: params[k] for k in ("zoom_tile", "share_chunk", "clip_batch")},
+            "tuning": {"zoom": {k: params[k] for k in ("zoom_tile", "item_pairs", "share_chunk", "clip_batch")},
                        **{k: v for k, v in tinfo.items() if k != "key"}}}
 
 

@@ -229,6 +229,9 @@ typedef struct {
     int ctas_per_sm;         /* CTAs per SM of the persistent leaf launch, 1..2 (2)                 */
     uint64_t route_capacity; /* ill-conditioned tets one launch may list; more set ADECO_ERR_LIMIT
                                 (0: automatic, max(65536, 256 x work items))                         */
+    uint32_t item_pairs;     /* zoom grids: a request's tile edge is zoom_tile halved (down to 8)
+                                while a work item would hold more expected candidate pairs than this,
+                                4096..2^26 (2^18)                                                     */
 } adeco_tuning;
 int adeco_session_get_tuning(adeco_session *s, adeco_tuning *t);
 int adeco_session_set_tuning(adeco_session *s, const adeco_tuning *t);

@@ -5,7 +5,7 @@
 //   2. the mirrored coordinate is 1 - x to within its own final rounding;
 //   3. double-float: TwoSum and TwoProd are exact, a share of identity
 //      weights is exactly 1.
-#include "../adeco_gb300/csrc/clip_engine.cuh"
+#include "../adeco_gb300/csrc/kernels.cuh"
 
 #include <cmath>
 #include <cstdio>
@@ -58,5 +58,29 @@ int main()
     const bool ok_share = one.hi == 1.f && one.lo == 0.f;
     std::printf("share of identity weights == 1: %s\n", ok_share ? "ok" : "FAIL");
     failures += !ok_share;
+
+    // the packed-immediate lookups equal the tables they stand for
+    int bad_tab = 0;
+    for (int m = 0; m < 16; ++m) bad_tab += (split_perm(m) != h_split_perm[m]) + (split_kin(m) != h_split_kin[m]);
+    for (int t = 0; t < 6; ++t)
+        for (int q = 0; q < 4; ++q) bad_tab += tet_conn(t, q) != h_tet_conn[t][q];
+    for (int c = 0; c < 8; ++c)
+        for (int a = 0; a < 3; ++a) bad_tab += ref_corner(c, a) != h_ref_corner[c][a];
+    std::printf("packed table lookups equal the tables: %s (%d)\n", bad_tab ? "FAIL" : "ok", bad_tab);
+    failures += bad_tab != 0;
+
+    // pair_mass: one rounding of the fixed-point sum, no drift from truncation
+    double pm_bias = 0.0, pm_total = 0.0;
+    std::uniform_real_distribution<double> U01(0.0, 1.0);
+    for (long i = 0; i < 1000000; ++i) {
+        const long long v = vol_fixed((float)(U01(rng) * 6.0)) + vol_fixed((float)(U01(rng) * 0.5));
+        const float f6 = (float)(0.1 + U01(rng));
+        const double x = std::ldexp((double)v, -kVolShift) * (double)f6;
+        pm_bias += (double)pair_mass(v, f6) - x;
+        pm_total += x;
+    }
+    const bool ok_pm = std::fabs(pm_bias) < 1e-10 * pm_total;
+    std::printf("pair_mass unbiased: %s (%.2e relative)\n", ok_pm ? "ok" : "FAIL", pm_bias / pm_total);
+    failures += !ok_pm;
     return failures ? 1 : 0;
 }
