@@ -54,7 +54,7 @@ class Timing(C.Structure):
     _fields_ = [("kernel_ms", C.c_double), ("total_ms", C.c_double), ("launches", C.c_uint64), ("tets", C.c_uint64),
                 ("candidate_pairs", C.c_uint64), ("partial_pairs", C.c_uint64), ("cell_inside_pairs", C.c_uint64),
                 ("tet_inside_pairs", C.c_uint64), ("fp64_pairs", C.c_uint64), ("items", C.c_uint64),
-                ("routed_tets", C.c_uint64)]
+                ("routed_tets", C.c_uint64), ("serial_pieces", C.c_uint64)]
 
     def as_dict(self):
         return {n: (float(getattr(self, n)) if t is C.c_double else int(getattr(self, n))) for n, t in self._fields_}

@@ -434,6 +434,14 @@ long long clip_piece_serial(const float p0[12], int face0)
 }
 
 #ifdef __CUDACC__
+// warp-wide maximum of a non-negative int (butterfly of shuffles)
+__device__ __forceinline__ int warp_max(int v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
 constexpr int kPool = 56;    // pieces per warp pool (2 CTAs of 8 warps fit in an SM's shared memory)
 constexpr int kPairs = 128;  // partial pairs per warp list
 
@@ -488,21 +496,48 @@ __device__ __forceinline__ void clip_pairs(WarpPool &pool, int np, Build build, 
         next = min(np, next + (nneed - from_pool));
         if (!__any_sync(0xffffffffu, valid)) break;
         __syncwarp();
-        // one step
-        int npush = 0;
-        float c1[12], c2[12];
-        if (valid) {
-            int f = 0, mask = 0;
-            bool last = false;
-            const int code = piece_step(p, face, f, mask, &last);
+        // one step.  A lane about to split reserves room in the pool for its
+        // extra children first (a warp-wide scan); a lane whose children do
+        // not fit keeps its piece and steps again next round, while the other
+        // lanes finish pieces and idle lanes drain the pool.  The lanes that
+        // fit are a prefix of the scan.  Only when every lane holds a piece
+        // and none can move does one lane clip its piece alone (serially, with
+        // a local stack): letting every pushing lane of a full pool do that
+        // had put most of the fine-grid time into one-lane serial clipping.
+        int f = 0, mask = 0, code = 0;
+        bool last = false;
+        if (valid) code = piece_step(p, face, f, mask, &last);
+        const bool split = valid && code == 2 && !last;
+        const int want = (split && split_kin(mask) != 1) ? 2 : 0;  // children to push
+        int incl = want;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const bool defer = want && (top + incl > kPool);
+        const unsigned moving = __ballot_sync(0xffffffffu, valid && !defer);
+        const unsigned deferred = __ballot_sync(0xffffffffu, defer);
+        const bool stuck = moving == 0u && __ballot_sync(0xffffffffu, valid) == 0xffffffffu;
+        if (valid && !defer) {
             long long v = 0;
-            if (code == 2 && !last) {
-                float c0[12];
-                const int n = split_piece(p, mask, f, c0, c1, c2);
+            if (split) {
+                float c0[12], c1[12], c2[12];
+                split_piece(p, mask, f, c0, c1, c2);
 #pragma unroll
                 for (int x = 0; x < 12; ++x) p[x] = c0[x];
-                npush = n - 1;
                 face = f + 1;
+                if (want) {
+                    const int base = top + incl - want;
+                    const uint32_t m = (uint32_t)owner | ((uint32_t)face << 8);
+#pragma unroll
+                    for (int x = 0; x < 12; ++x) {
+                        pool.v[x][base] = c1[x];
+                        pool.v[x][base + 1] = c2[x];
+                    }
+                    pool.meta[base] = m;
+                    pool.meta[base + 1] = m;
+                }
             } else {
                 // finished, or at its last crossed face: the inside part
                 // needs no more clipping, so its volume is added here
@@ -510,37 +545,13 @@ __device__ __forceinline__ void clip_pairs(WarpPool &pool, int np, Build build, 
                 valid = false;
             }
             if (v) atomicAdd(reinterpret_cast<unsigned long long *>(&pool.vacc[owner]), (unsigned long long)v);
+        } else if (stuck && lane == __ffs(deferred) - 1) {
+            const long long acc = clip_piece_serial(p, face);
+            atomicAdd(reinterpret_cast<unsigned long long *>(&pool.vacc[owner]), (unsigned long long)acc);
+            valid = false;
+            ++fallbacks;
         }
-        // push the extra pieces (warp-wide exclusive scan of npush)
-        int incl = npush;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += y;
-        }
-        const int total = __shfl_sync(0xffffffffu, incl, 31);
-        if (total) {
-            if (top + total <= kPool) {
-                const int base = top + incl - npush;
-                const uint32_t m = (uint32_t)owner | ((uint32_t)face << 8);
-                if (npush >= 1) {
-#pragma unroll
-                    for (int x = 0; x < 12; ++x) pool.v[x][base] = c1[x];
-                    pool.meta[base] = m;
-                }
-                if (npush == 2) {
-#pragma unroll
-                    for (int x = 0; x < 12; ++x) pool.v[x][base + 1] = c2[x];
-                    pool.meta[base + 1] = m;
-                }
-                top += total;
-            } else if (npush) {  // pool full: finish this lane's extra pieces serially
-                long long acc = clip_piece_serial(c1, face);
-                if (npush == 2) acc += clip_piece_serial(c2, face);
-                atomicAdd(reinterpret_cast<unsigned long long *>(&pool.vacc[owner]), (unsigned long long)acc);
-                ++fallbacks;
-            }
-        }
+        top += warp_max((want && !defer) ? incl : 0);
         __syncwarp();
     }
     __syncwarp();
@@ -699,40 +710,36 @@ __device__ __forceinline__ void clip_bary_pairs(BaryPool &pool, int np, Build bu
         next = min(np, next + (nneed - from_pool));
         if (!__any_sync(0xffffffffu, valid)) break;
         __syncwarp();
-        // one step
-        int npush = 0, k = 1;
-        bool split = false;
-        float P[4][7], E[4][7];
-        if (valid) {
-            int f = 0, mask = 0;
-            bool last = false;
-            const int code = bary_step(r, face, f, mask, last);
-            F2 c = {0.f, 0.f};
-            if (code == 2 && !last) {
-                bary_split(r, f, mask, P, E, k);
-                split = true;
-                npush = (k == 1) ? 0 : 2;
-                face = f + 1;
-            } else {
-                if (code == 1) c = bary_share(r);
-                if (code == 2) c = f2_mul_f(bary_share(r), bary_last_fraction(r, f, mask));
-                valid = false;
-            }
-            const long long v = share_fixed(c);
-            if (v) atomicAdd(reinterpret_cast<unsigned long long *>(&pool.acc[owner]), (unsigned long long)v);
-        }
-        // push children 1 and 2 (warp-wide exclusive scan of npush)
-        int incl = npush;
+        // one step, with the main engine's pool reservation: a lane whose two
+        // extra children do not fit keeps its piece for the next round; one
+        // lane clips serially only when every lane holds a piece and none can
+        // move
+        int f = 0, mask = 0, code = 0;
+        bool last = false;
+        if (valid) code = bary_step(r, face, f, mask, last);
+        const bool want_split = valid && code == 2 && !last;
+        const int want = (want_split && split_kin(mask) != 1) ? 2 : 0;
+        int incl = want;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const int y = __shfl_up_sync(0xffffffffu, incl, o);
             if (lane >= o) incl += y;
         }
-        const int total = __shfl_sync(0xffffffffu, incl, 31);
-        if (total) {
-            if (top + total <= kBaryPool) {
-                if (npush) {
-                    const int base = top + incl - npush;
+        const bool defer = want && (top + incl > kBaryPool);
+        const unsigned moving = __ballot_sync(0xffffffffu, valid && !defer);
+        const unsigned deferred = __ballot_sync(0xffffffffu, defer);
+        const bool stuck = moving == 0u && __ballot_sync(0xffffffffu, valid) == 0xffffffffu;
+        int k = 1;
+        bool split = false;
+        float P[4][7], E[4][7];
+        if (valid && !defer) {
+            F2 c = {0.f, 0.f};
+            if (want_split) {
+                bary_split(r, f, mask, P, E, k);
+                split = true;
+                face = f + 1;
+                if (want) {
+                    const int base = top + incl - want;
                     const uint32_t m = (uint32_t)owner | ((uint32_t)face << 8);
 #pragma unroll
                     for (int x = 0; x < kBaryRec; ++x) {
@@ -742,21 +749,20 @@ __device__ __forceinline__ void clip_bary_pairs(BaryPool &pool, int np, Build bu
                     pool.meta[base] = m;
                     pool.meta[base + 1] = m;
                 }
-                top += total;
-            } else if (npush) {  // pool full: finish this lane's extra pieces serially
-                float rec[kBaryRec];
-                F2 acc = {0.f, 0.f};
-#pragma unroll
-                for (int c = 1; c <= 2; ++c) {
-#pragma unroll
-                    for (int x = 0; x < kBaryRec; ++x) rec[x] = bary_child(P, E, k, c, x);
-                    acc = f2_add(acc, clip_bary_serial(rec, face));
-                }
-                atomicAdd(reinterpret_cast<unsigned long long *>(&pool.acc[owner]),
-                          (unsigned long long)share_fixed(acc));
-                ++fallbacks;
+            } else {
+                if (code == 1) c = bary_share(r);
+                if (code == 2) c = f2_mul_f(bary_share(r), bary_last_fraction(r, f, mask));
+                valid = false;
             }
+            const long long v = share_fixed(c);
+            if (v) atomicAdd(reinterpret_cast<unsigned long long *>(&pool.acc[owner]), (unsigned long long)v);
+        } else if (stuck && lane == __ffs(deferred) - 1) {
+            atomicAdd(reinterpret_cast<unsigned long long *>(&pool.acc[owner]),
+                      (unsigned long long)share_fixed(clip_bary_serial(r, face)));
+            valid = false;
+            ++fallbacks;
         }
+        top += warp_max((want && !defer) ? incl : 0);
         if (split) {
 #pragma unroll
             for (int x = 0; x < kBaryRec; ++x) r[x] = bary_child(P, E, k, 0, x);

@@ -604,9 +604,11 @@ float halfspace_pair_vol6(const WarpTets &W, const GridDesc &g, int s, int a, in
 }
 
 // Non-negative mass of a pair (FP32, about 1e-7 relative) -> the cell's
-// 64-bit fixed-point accumulator, with integer operations only.
-__device__ __noinline__ void scatter(const DepositParams &P, const GridDesc &g, const WarpTets &W, int s, int a,
-                                     int b, int c, float m)
+// 64-bit fixed-point accumulator, with integer operations only.  Inlined: as
+// a call it made the pair loop save and restore its live registers in local
+// memory around every scatter (C2: 16% of the kernel time).
+__device__ __forceinline__ void scatter(const DepositParams &P, const GridDesc &g, const WarpTets &W, int s, int a,
+                                        int b, int c, float m)
 {
     const unsigned long long fx = to_fixed(m, g.shift);
     if (fx == 0ull) return;

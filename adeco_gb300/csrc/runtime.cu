@@ -1129,6 +1129,7 @@ extern "C" int adeco_session_deposit_leaves(adeco_session *s, int precision, dou
             timing->cell_inside_pairs = st[ST_CELLIN];
             timing->tet_inside_pairs = st[ST_INSIDE];
             timing->fp64_pairs = st[ST_FP64];
+            timing->serial_pieces = st[ST_FALLBACK];
         }
     }
     if (host_out) CUDA_TRY(cudaMemcpy(host_out, s->d_out.p, s->out_values * sizeof(double), cudaMemcpyDeviceToHost));

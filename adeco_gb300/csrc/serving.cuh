@@ -465,22 +465,46 @@ static int server_get(adeco_session *s, Server *&out)
     return ADECO_OK;
 }
 
-// Tile edge of a request grid of d cells per axis whose tets are r cells
-// wide (lattice spacing over cell size): the tuned edge `tile`, halved down
-// to 8 while one (tile, meta-cell) item is expected to hold more than
-// `item_pairs` candidate pairs -- the meta-cell's tets that reach a tile of
-// T cells, 6 (T/r + 1)^3 of at most 2058, each meeting min(T, r + 1)^3 of its
-// cells.  On fine grids an item of a 64^3 tile held ~1e7 pairs: one CTA
-// carried it for tens of milliseconds while the rest of the GPU idled.
-static int request_tile(int tile, double item_pairs, int d, double r)
+// Work-item shape of a request grid of d cells per axis whose tets are r
+// cells wide (lattice spacing over cell size): an item is (tile of T cells
+// per axis, block of e^3 cubes of one meta-cell).  Expected candidate pairs
+// of an item: the block's tets that reach the tile, 6 min(e, T/r + 1)^3,
+// each meeting min(T, r + 1)^3 of the tile's cells.  The item target W is the
+// request's expected pairs spread over 4 waves of the GPU's CTA slots, within
+// [2^14, item_pairs]; of the shapes (T = the tuned edge halved down to 8,
+// e = 7, 4 or 2) whose items stay under W, the one with the fewest items is
+// taken (none: the smallest items).  One (tile, meta-cell) item of a 64^3
+// tile held ~1e7 pairs on fine grids, and ~1e5 on tet-sized cells where a
+// 128^3 request then had ~800 items: a few waves of long items whose tail
+// left most of the GPU idle.
+struct ItemShape {
+    int tile, cubes;
+};
+static ItemShape request_shape(int tile, double item_pairs, int slots, int d, double r, double req_pairs)
 {
-    int T = std::max(1, std::min(tile, d));
-    auto pairs = [r](int t) {
-        const double tets = std::min(2058.0, 6.0 * std::pow((double)t / r + 1.0, 3.0));
-        return tets * std::pow(std::min((double)t, r + 1.0), 3.0);
-    };
-    while (T > 8 && pairs(T) > item_pairs) T = (T + 1) / 2;
-    return T;
+    const double W = std::min(item_pairs, std::max(16384.0, req_pairs / (4.0 * slots)));
+    ItemShape best{std::max(1, std::min(tile, d)), kMetaCubes};
+    double best_items = -1.0, best_est = 1e300;
+    bool feasible = false;
+    for (int T = std::max(1, std::min(tile, d));; T = (T + 1) / 2) {
+        for (int e : {kMetaCubes, 4, 2}) {
+            const double reach = std::min((double)e, (double)T / r + 1.0);
+            const double est = 6.0 * reach * reach * reach * std::pow(std::min((double)T, r + 1.0), 3.0);
+            const double tiles = std::pow(std::ceil((double)d / T), 3.0);
+            const double metas = std::pow((double)T / (kMetaCubes * r) + 1.0, 3.0);
+            const double blocks = std::pow(std::ceil((double)kMetaCubes / e), 3.0);
+            const double items = tiles * metas * blocks;
+            if (est <= W) {
+                if (!feasible || items < best_items) best = {T, e}, best_items = items;
+                feasible = true;
+            } else if (!feasible && est < best_est) {
+                best = {T, e};
+                best_est = est;
+            }
+        }
+        if (T <= 8) break;
+    }
+    return best;
 }
 
 static void request_box(const adeco_request &r, float bb[6])
@@ -588,7 +612,12 @@ extern "C" int adeco_session_submit(adeco_session *s, const adeco_request *reqs,
         // cover very many cells, and one item per meta-cell would leave all
         // of that to a single CTA.  The tile edge is the tuned one, halved
         // while an item's expected candidate pairs exceed item_pairs.
-        const int tile_d = request_tile(tile, item_pairs, d, S->spacing / ((double)reqs[i].side / d));
+        const double r_cells = S->spacing / ((double)reqs[i].side / d);  // tet width in cells
+        const double per_side = (double)reqs[i].side / S->spacing + (double)d;
+        const double req_pairs = 6.0 * per_side * per_side * per_side;  // 6 tets per cube x (1 + r)^3 cells each
+        const ItemShape shape = request_shape(tile, item_pairs, s->dp.sms * s->dp.mixed_blocks_per_sm, d, r_cells,
+                                              req_pairs);
+        const int tile_d = shape.tile, eb = shape.cubes;
         const int nt = (d + tile_d - 1) / tile_d;
         const size_t first_grid = j.grids.size(), first = j.items.size();
         for (int tz = 0; tz < nt; ++tz)
@@ -612,11 +641,18 @@ extern "C" int adeco_session_submit(adeco_session *s, const adeco_request *reqs,
                     for (const uint32_t id : hits) {
                         int org[3], nv[3];
                         s->meta.range(id, org, nv);
-                        Item it;
-                        it.base = org[0] + (long long)s->nx * (org[1] + (long long)s->ny * org[2]);
-                        it.grid = grid_index;
-                        it.nv = nv[0] | (nv[1] << 8) | (nv[2] << 16);
-                        j.items.push_back(it);
+                        // blocks of at most eb^3 of the meta-cell's cubes
+                        for (int bz = 0; bz < nv[2] - 1; bz += eb)
+                            for (int by = 0; by < nv[1] - 1; by += eb)
+                                for (int bx = 0; bx < nv[0] - 1; bx += eb) {
+                                    const int vx = std::min(eb, nv[0] - 1 - bx) + 1, vy = std::min(eb, nv[1] - 1 - by) + 1,
+                                              vz = std::min(eb, nv[2] - 1 - bz) + 1;
+                                    Item it;
+                                    it.base = (org[0] + bx) + (long long)s->nx * ((org[1] + by) + (long long)s->ny * (org[2] + bz));
+                                    it.grid = grid_index;
+                                    it.nv = vx | (vy << 8) | (vz << 16);
+                                    j.items.push_back(it);
+                                }
                     }
                 }
         // fixed-point scale from the tets the request can see (all its tiles)
@@ -630,14 +666,19 @@ extern "C" int adeco_session_submit(adeco_session *s, const adeco_request *reqs,
         j.rtab.push_back(r);
         // expected candidate pairs: 6 tets per lattice cube over the box, each
         // meeting (1 + spacing / cell)^3 cells
-        const double per_side = (double)reqs[i].side / S->spacing + (double)d;
-        j.est_pairs += 6.0 * per_side * per_side * per_side;
+        j.est_pairs += req_pairs;
         off += (long long)d * d * d;
     }
     j.cells = (size_t)off;
     j.level = j.est_pairs < 2e7 ? 0 : (j.est_pairs < 1.5e8 ? 1 : 2);
     // layout of the job's block
-    unsigned long long rcap = route_capacity((long long)j.items.size());
+    // route list: the allocating paths' rule (an eighth of a whole meta-cell's
+    // 2058 tets per item, at least 65536) counted in cubes, since a request's
+    // items may hold smaller blocks
+    long long cubes = 0;
+    for (const Item &it : j.items)
+        cubes += (long long)((it.nv & 0xff) - 1) * (((it.nv >> 8) & 0xff) - 1) * (((it.nv >> 16) & 0xff) - 1);
+    unsigned long long rcap = route_capacity((cubes * 6 / 8 + 255) / 256);
     if (s->tuning.route_capacity) rcap = std::min<unsigned long long>(rcap, s->tuning.route_capacity);
     j.rcap = rcap;
     j.off_stat = round_up(j.cells * sizeof(unsigned long long), 16);

@@ -203,6 +203,8 @@ typedef struct {
     uint64_t items;         /* work items (grid x vertex block)                       */
     uint64_t routed_tets;   /* ill-conditioned tets (longest edge^3 > 32 |6V|) that the
                                barycentric route deposited                          */
+    uint64_t serial_pieces; /* pieces a lane clipped alone because its warp's piece
+                               pool was full and no lane could move (collect_stats) */
 } adeco_timing;
 
 /* Deposit every leaf (leaf_dims^3 cells over the leaf's cube) in one batched
