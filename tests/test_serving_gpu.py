@@ -61,8 +61,12 @@ def test_batches_queue_inside_the_library(adeco, lattice64):
             b = s.submit([r])
             alone.append(s.result(b, 0, 96))
             s.release(b)
+    import re
+    with adeco.Session(lattice64, hbm_fraction=1e-9) as s:  # the library states what one batch needs
+        with pytest.raises(adeco.AdecoError) as e:
+            s.submit([reqs[0]])
+        one = int(re.search(r"needs (\d+) bytes", str(e.value)).group(1))
     free, _ = torch.cuda.mem_get_info()
-    one = 96 ** 3 * 8 + 65537 * 8 + (1 << 20)  # results + route list + items and descriptors
     with adeco.Session(lattice64, hbm_fraction=1.5 * one / free) as s:
         ids = [s.submit([r]) for r in reqs]
         for b, want in zip(ids, alone):
