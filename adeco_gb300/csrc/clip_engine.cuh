@@ -546,7 +546,13 @@ __device__ __forceinline__ void clip_pairs(WarpPool &pool, int np, Build build, 
             }
             if (v) atomicAdd(reinterpret_cast<unsigned long long *>(&pool.vacc[owner]), (unsigned long long)v);
         } else if (stuck && lane == __ffs(deferred) - 1) {
-            const long long acc = clip_piece_serial(p, face);
+            // a copy made here: handing p itself to the out-of-line routine
+            // takes its address, and p then lives in local memory, stored
+            // there on every step although this branch almost never runs
+            float q[12];
+#pragma unroll
+            for (int x = 0; x < 12; ++x) q[x] = p[x];
+            const long long acc = clip_piece_serial(q, face);
             atomicAdd(reinterpret_cast<unsigned long long *>(&pool.vacc[owner]), (unsigned long long)acc);
             valid = false;
             ++fallbacks;
@@ -757,8 +763,11 @@ __device__ __forceinline__ void clip_bary_pairs(BaryPool &pool, int np, Build bu
             const long long v = share_fixed(c);
             if (v) atomicAdd(reinterpret_cast<unsigned long long *>(&pool.acc[owner]), (unsigned long long)v);
         } else if (stuck && lane == __ffs(deferred) - 1) {
+            float q[kBaryRec];  // a copy, so that r itself never needs an address (see clip_pairs)
+#pragma unroll
+            for (int x = 0; x < kBaryRec; ++x) q[x] = r[x];
             atomicAdd(reinterpret_cast<unsigned long long *>(&pool.acc[owner]),
-                      (unsigned long long)share_fixed(clip_bary_serial(r, face)));
+                      (unsigned long long)share_fixed(clip_bary_serial(q, face)));
             valid = false;
             ++fallbacks;
         }

@@ -259,8 +259,7 @@ ADECO_HD inline int setup_tet(const float3 vin[4], const float ghin[4][3], const
         }
     }
     // orientation rule on the vertex order: swap 0 <-> 3 when negative
-    const int o0 = (sgn < 0) ? 3 : 0, o3 = (sgn < 0) ? 0 : 3;
-    const int ord[4] = {o0, 1, 2, o3};
+    const bool swap03 = sgn < 0;  // selects, not an index: an indexed vertex array would live in local memory
     // Tight range: of the candidate cells [lo, hi], only those whose box
     // [c r, c r + 1] (grid frame) meets the tet's AABB can receive mass (the
     // rest fail the AABB test).  Bounds widened by the FP32 rounding of the
@@ -278,7 +277,12 @@ ADECO_HD inline int setup_tet(const float3 vin[4], const float ghin[4][3], const
         lo[a] = c0;
         hi[a] = c1;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) shift_frame(ghin[ord[q]][a], glin[ord[q]][a], c0, g.drcell[a], qf[q][a], ql[q][a]);
+        for (int q = 0; q < 4; ++q) {
+            const int src = (q == 0) ? 0 : ((q == 3) ? 3 : q);  // the vertex before the orientation swap
+            const float h = (q == 0 || q == 3) ? (swap03 ? ghin[3 - src][a] : ghin[src][a]) : ghin[q][a];
+            const float l = (q == 0 || q == 3) ? (swap03 ? glin[3 - src][a] : glin[src][a]) : glin[q][a];
+            shift_frame(h, l, c0, g.drcell[a], qf[q][a], ql[q][a]);
+        }
     }
     // |6 V| in the anchor frame from the FP32 pairs, in double-float (the
     // tet's volume normaliser): edge vectors from vertex 3, then the triple
