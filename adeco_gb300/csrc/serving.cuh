@@ -40,6 +40,9 @@ inline size_t round_up(size_t n, size_t a) { return (n + a - 1) / a * a; }
 // pinned host memory with the launch; larger ones keep them on the device.
 constexpr size_t kEagerBytes = size_t(1) << 30;
 
+// expected-pair boundaries of the three priority classes of batches
+constexpr double kClassPairs[2] = {1.6e7, 3.0e7};
+
 // First-fit allocator over a few large chunks of device or pinned host memory.
 struct Arena {
     struct Chunk {
@@ -206,6 +209,10 @@ struct ServeJob {
 struct Server {
     adeco_session *s = nullptr;
     static constexpr int kLevels = 3, kPerLevel = 4;
+    // streams a class may use at once: cheap batches share the GPU freely;
+    // the most expensive class runs one batch at a time (first in, first
+    // out), each at full speed, instead of several slowing each other down
+    static constexpr int kUsable[kLevels] = {4, 2, 1};
     cudaStream_t streams[kLevels * kPerLevel] = {};
     bool stream_busy[kLevels * kPerLevel] = {};
     std::mutex mu;                 // jobs, queue, arenas, streams
@@ -286,7 +293,7 @@ static std::vector<ServeJob *> admit_locked(Server &S)
     for (auto it = S.pending.begin(); it != S.pending.end();) {
         ServeJob &j = **it;
         int slot = -1;
-        for (int k = 0; k < Server::kPerLevel && slot < 0; ++k) {
+        for (int k = 0; k < Server::kUsable[j.level] && slot < 0; ++k) {
             const int q = j.level * Server::kPerLevel + k;
             if (!S.stream_busy[q]) slot = q;
         }
@@ -670,7 +677,10 @@ extern "C" int adeco_session_submit(adeco_session *s, const adeco_request *reqs,
         off += (long long)d * d * d;
     }
     j.cells = (size_t)off;
-    j.level = j.est_pairs < 2e7 ? 0 : (j.est_pairs < 1.5e8 ? 1 : 2);
+    // priority class from the expected pairs (128^3 requests: side below ~4
+    // lattice spacings' worth of units take ~1-5 ms alone, up to ~15 units
+    // ~13 ms, larger ~24 ms on a GB300)
+    j.level = j.est_pairs < kClassPairs[0] ? 0 : (j.est_pairs < kClassPairs[1] ? 1 : 2);
     // layout of the job's block
     // route list: the allocating paths' rule (an eighth of a whole meta-cell's
     // 2058 tets per item, at least 65536) counted in cubes, since a request's

@@ -488,6 +488,11 @@ def run_ours(args, rank, ws, local):
         sv = serve_leg(args, pos)
         line["serve"] = sv
         line["serve_p50_ms"], line["serve_p99_ms"] = sv["p50_ms"], sv["p99_ms"]
+        line["serve_rate_req_s"] = sv["offered_rate"]
+        if args.serve_rate_high:  # a second, heavier load point
+            hi = serve_leg(args, pos, args.serve_rate_high)
+            line["serve_high"] = {k: hi[k] for k in ("offered_rate", "achieved_rate", "p50_ms", "p90_ms", "p99_ms",
+                                                     "max_ms", "requests", "unfinished_at_deadline")}
     if ws == 1 and not args.skip_zoom:
         zm = zoom_leg(args, pos)
         line["zoom"] = zm
@@ -547,21 +552,21 @@ def oracle_leaf_check(pos, n, grids, nodes, off, ids, leaves, count):
     return out
 
 
-def serve_leg(args, pos):
+def serve_leg(args, pos, rate=None):
     """Poisson stream of 128^3-cell zoom requests against the resident lattice."""
     from adeco_gb300 import deposit as D
     from adeco_gb300.synthetic import poisson_requests
-    stream = poisson_requests(args.serve_rate, args.serve_seconds, L=L_BOX, seed=SERVE_SEED,
-                              dims=tuple(args.serve_dims))
+    rate = args.serve_rate if rate is None else rate
+    stream = poisson_requests(rate, args.serve_seconds, L=L_BOX, seed=SERVE_SEED, dims=tuple(args.serve_dims))
     with D.Session(pos, device=args.device) as s:
         res = serve_stream(s, stream, args.serve_seconds + args.serve_drain_s)
     lat = np.sort(np.asarray(res["lat"]))
-    return {"workload": f"Poisson arrivals at {args.serve_rate:g} req/s for {args.serve_seconds:g} s (seed "
+    return {"workload": f"Poisson arrivals at {rate:g} req/s for {args.serve_seconds:g} s (seed "
                         f"{SERVE_SEED}): zoom boxes, centre uniform, side log-uniform [0.005L, 0.5L], resolution "
                         f"from {args.serve_dims}; one batch per request, submitted at its arrival",
             "p50_ms": float(np.percentile(lat, 50)), "p90_ms": float(np.percentile(lat, 90)),
             "p99_ms": float(np.percentile(lat, 99)), "max_ms": float(lat[-1]), "requests": int(lat.size),
-            "offered_rate": args.serve_rate, "achieved_rate": lat.size / res["wall"],
+            "offered_rate": rate, "achieved_rate": lat.size / res["wall"],
             "unfinished_at_deadline": res["unfinished"], "serving_stats": res["stats"]}
 
 
@@ -811,7 +816,8 @@ def main():
     ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c4", "zoom", "serve"])
     ap.add_argument("--zoom-dims", type=int, nargs="+", default=[32, 64, 128, 256])
     ap.add_argument("--zoom-count", type=int, default=ZOOM_COUNT)
-    ap.add_argument("--serve-rate", type=float, default=100.0)
+    ap.add_argument("--serve-rate", type=float, default=30.0)
+    ap.add_argument("--serve-rate-high", type=float, default=50.0, help="default run: a second serving load point (0: none)")
     ap.add_argument("--serve-seconds", type=float, default=8.0)
     ap.add_argument("--serve-dims", type=int, nargs="+", default=[128])
     ap.add_argument("--serve-drain-s", type=float, default=30.0)
