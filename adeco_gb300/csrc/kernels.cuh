@@ -537,9 +537,9 @@ int classify_fp64(const WarpTets &W, const GridDesc &g, int s, int a, int b, int
     return all_in ? P_CELL_INSIDE : P_PARTIAL;
 }
 
-// cross: the one tet face plane the cell straddles when the cell is certainly
-// inside the other three (then cell ∩ tet = cell ∩ that face's half-space),
-// else -1.
+// cross: the tet face planes the cell straddles when the cell is certainly
+// inside the others -- then cell ∩ tet = cell ∩ their half-spaces: one face f
+// (cross = f) or two faces f1 < f2 (cross = f1 + 4 (f2 + 1)); else -1.
 ADECO_HD inline int classify_pair(const WarpTets &W, const GridDesc &g, int s, int a, int b, int c, bool &used_fp64,
                                   int &cross)
 {
@@ -553,7 +553,7 @@ ADECO_HD inline int classify_pair(const WarpTets &W, const GridDesc &g, int s, i
         W.bmin[2][s] >= fc && W.bmax[2][s] <= fc + 1.f)
         return P_TET_INSIDE;
     bool all_in = true, unsure = false;
-    int ncross = 0, fcross = 0;
+    int ncross = 0, fcross = 0, ffirst = 0;
     const float t = W.tol[s];
 #pragma unroll
     for (int f = 0; f < 4; ++f) {
@@ -566,6 +566,7 @@ ADECO_HD inline int classify_pair(const WarpTets &W, const GridDesc &g, int s, i
         if (mx <= t) unsure = true;
         if (mn > t) continue;
         all_in = false;
+        if (ncross == 0) ffirst = f;
         ++ncross;
         fcross = f;
         if (mn > -t) unsure = true;
@@ -575,24 +576,19 @@ ADECO_HD inline int classify_pair(const WarpTets &W, const GridDesc &g, int s, i
         return classify_fp64(W, g, s, a, b, c);
     }
     if (ncross == 1) cross = fcross;
+    if (ncross == 2) cross = ffirst + 4 * (fcross + 1);
     return all_in ? P_CELL_INSIDE : P_PARTIAL;
 }
 
-// 6x volume of cell (a, b, c) ∩ slot s's tet when the cell straddles only
-// face f.  The face's linear function G(u) = n . (cell origin + u - centroid)
-// is taken about the face's centroid, so that the FP32 rounding of its normal
-// only turns the plane about the centroid: the volume a slightly turned plane
-// adds on one side of the centroid it removes on the other, and the tet's mass
-// stays conserved over its cells.  Its value at the cell origin, n . origin -
-// (d + dlo), cancels terms as large as the tet is wide in cells: it is formed
-// exactly in double-float (TwoProd of n with the integer cell offsets) and
-// rounded once.
-#ifdef __CUDA_ARCH__
-__device__ __noinline__
-#else
-inline
-#endif
-float halfspace_pair_vol6(const WarpTets &W, const GridDesc &g, int s, int a, int b, int c, int f)
+// Value at the origin of cell (a, b, c) of face f's linear function G(u) =
+// n . (cell origin + u - centroid), taken about the face's centroid so that
+// the FP32 rounding of its normal only turns the plane about the centroid:
+// the volume a slightly turned plane adds on one side of the centroid it
+// removes on the other, and the tet's mass stays conserved over its cells.
+// n . origin - (d + dlo) cancels terms as large as the tet is wide in cells:
+// it is formed exactly in double-float (TwoProd of n with the integer cell
+// offsets) and rounded once.
+ADECO_HD inline float face_value_at_cell(const WarpTets &W, const GridDesc &g, int s, int a, int b, int c, int f)
 {
     const int cc[3] = {a, b, c};
     F2 G = {-W.d[f][s], -W.dlo[f][s]};
@@ -603,8 +599,25 @@ float halfspace_pair_vol6(const WarpTets &W, const GridDesc &g, int s, int a, in
         G = f2_add(G, f2_two_prod(nx, fc));
         small = fmaf(nx * fc, g.drcell[x], small);
     }
-    const float G0 = G.hi + (G.lo + small);
-    return halfspace_cube_vol6(G0, W.n[f][0][s], W.n[f][1][s], W.n[f][2][s]);
+    return G.hi + (G.lo + small);
+}
+
+// 6x volume of cell (a, b, c) ∩ slot s's tet when the cell straddles only the
+// face(s) `cross` names (classify_pair): one face, the cube's part on its
+// inside; two faces, the part inside both.
+#ifdef __CUDA_ARCH__
+__device__ __noinline__
+#else
+inline
+#endif
+float facecut_pair_vol6(const WarpTets &W, const GridDesc &g, int s, int a, int b, int c, int cross)
+{
+    const int f1 = cross & 3, f2 = (cross >> 2) - 1;
+    const float G1 = face_value_at_cell(W, g, s, a, b, c, f1);
+    if (f2 < 0) return halfspace_cube_vol6(G1, W.n[f1][0][s], W.n[f1][1][s], W.n[f1][2][s]);
+    const float G2 = face_value_at_cell(W, g, s, a, b, c, f2);
+    return twoplane_cube_vol6(G1, W.n[f1][0][s], W.n[f1][1][s], W.n[f1][2][s], G2, W.n[f2][0][s], W.n[f2][1][s],
+                              W.n[f2][2][s]);
 }
 
 // Non-negative mass of a pair (FP32, about 1e-7 relative) -> the cell's
@@ -807,8 +820,8 @@ __device__ __forceinline__ void pair_range(const DepositParams &P, const GridDes
             } else if (cls == P_PARTIAL) {
                 ++st.part;
                 ++st.bbox;
-                if (cross >= 0) {  // one face cuts the cell: closed form, no clipping
-                    const float dm = halfspace_pair_vol6(Wc, g, s, a, b, c, cross) * Wc.f6[s];
+                if (cross >= 0) {  // one or two faces cut the cell: closed form, no clipping
+                    const float dm = facecut_pair_vol6(Wc, g, s, a, b, c, cross) * Wc.f6[s];
                     if (dm > 0.f) scatter(P, g, Wc, s, a, b, c, dm);
                 } else {
                     part = true;
