@@ -198,16 +198,33 @@ ADECO_HD inline float inside_fraction(const float p[12], int mask, int f)
     return side_fraction(x0, x1, x2, x3, mask, (f & 1) ? 1.f : 0.f);
 }
 
-// 6x volume of the unit cube's part where G(u) = G0 + n.u > 0: the cube is
-// split into the 6 tets around its diagonal (0,0,0)-(1,1,1), each of 6x
-// volume 1, and each tet's inside fraction comes from the values of G at its
-// vertices -- non-negative terms only, so no cancellation, and the same
-// arithmetic for every lane.
-ADECO_HD inline float halfspace_cube_vol6(float G0, float nx, float ny, float nz)
+// Values of a linear function G(u) = G0 + n.u at the unit cube's 8 corners
+// (k: bit 0 x, bit 1 y, bit 2 z) from G0 as a double-float pair: each corner
+// value is formed exactly (TwoSum) and rounded once, so that a value near
+// zero -- a plane passing close to a corner, a thin sliver of the cube --
+// keeps its relative precision instead of the ~6e-8 |n| of an FP32 sum.
+ADECO_HD inline void cube_corner_values(F2 G0, float nx, float ny, float nz, float P[8])
 {
-    float G[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) G[k] = G0 + ((k & 1) ? nx : 0.f) + ((k & 2) ? ny : 0.f) + ((k & 4) ? nz : 0.f);
+    const F2 g1 = f2_add(G0, F2{nx, 0.f}), g2 = f2_add(G0, F2{ny, 0.f}), g4 = f2_add(G0, F2{nz, 0.f});
+    const F2 g3 = f2_add(g1, F2{ny, 0.f}), g5 = f2_add(g1, F2{nz, 0.f}), g6 = f2_add(g2, F2{nz, 0.f});
+    const F2 g7 = f2_add(g3, F2{nz, 0.f});
+    P[0] = G0.hi + G0.lo;
+    P[1] = g1.hi;
+    P[2] = g2.hi;
+    P[3] = g3.hi;
+    P[4] = g4.hi;
+    P[5] = g5.hi;
+    P[6] = g6.hi;
+    P[7] = g7.hi;
+}
+
+// 6x volume of the unit cube's part where G > 0, from G's values at the 8
+// corners: the cube is split into the 6 tets around its diagonal
+// (0,0,0)-(1,1,1), each of 6x volume 1, and each tet's inside fraction comes
+// from G's values at its vertices -- non-negative terms only, so no
+// cancellation, and the same arithmetic for every lane.
+ADECO_HD inline float halfspace_cube_vol6(const float G[8])
+{
     const int in0 = (int)(G[0] > 0.f), in7 = (int)(G[7] > 0.f);
     const int path[6][2] = {{1, 3}, {1, 5}, {2, 3}, {2, 6}, {4, 5}, {4, 6}};
     float v = 0.f;
@@ -235,9 +252,9 @@ ADECO_HD inline float plane_fraction(float b0, float b1, float b2, float b3)
     return m == 15 ? 1.f : (m == 0 ? 0.f : side_fraction(b0, b1, b2, b3, m, 0.f));
 }
 
-// 6x volume of the unit cube's part where both G1(u) = G01 + n1.u > 0 and
-// G2(u) = G02 + n2.u > 0 -- a cell that two tet faces cut, inside the other
-// two.  Each of the cube's 6 diagonal (Kuhn) tets, of 6x volume 1, is cut by
+// 6x volume of the unit cube's part where both G1 > 0 and G2 > 0, from their
+// values at the 8 corners (cube_corner_values) -- a cell that two tet faces
+// cut, inside the other two.  Each of the cube's 6 diagonal (Kuhn) tets, of 6x volume 1, is cut by
 // plane 1 into 1 or 3 sub-tets, split_piece's patterns over the inside-first
 // vertices A B C D (k inside):
 //   k = 1: (A, Xab, Xac, Xad)                          weight tAB tAC tAD
@@ -249,15 +266,8 @@ ADECO_HD inline float plane_fraction(float b0, float b1, float b2, float b3)
 // plane 1 and u = 1 - t), and each sub-tet's part inside plane 2 comes from
 // plane 2's values at its vertices -- interpolated along the same edges -- by
 // plane_fraction.  Non-negative terms only: no cancellation, as for one face.
-ADECO_HD inline float twoplane_cube_vol6(float G01, float n1x, float n1y, float n1z, float G02, float n2x, float n2y,
-                                         float n2z)
+ADECO_HD inline float twoplane_cube_vol6(const float P1[8], const float P2[8])
 {
-    float P1[8], P2[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        P1[k] = G01 + ((k & 1) ? n1x : 0.f) + ((k & 2) ? n1y : 0.f) + ((k & 4) ? n1z : 0.f);
-        P2[k] = G02 + ((k & 1) ? n2x : 0.f) + ((k & 2) ? n2y : 0.f) + ((k & 4) ? n2z : 0.f);
-    }
     const int path[6][2] = {{1, 3}, {1, 5}, {2, 3}, {2, 6}, {4, 5}, {4, 6}};
     float v = 0.f;
 #pragma unroll

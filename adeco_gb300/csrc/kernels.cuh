@@ -587,8 +587,8 @@ ADECO_HD inline int classify_pair(const WarpTets &W, const GridDesc &g, int s, i
 // removes on the other, and the tet's mass stays conserved over its cells.
 // n . origin - (d + dlo) cancels terms as large as the tet is wide in cells:
 // it is formed exactly in double-float (TwoProd of n with the integer cell
-// offsets) and rounded once.
-ADECO_HD inline float face_value_at_cell(const WarpTets &W, const GridDesc &g, int s, int a, int b, int c, int f)
+// offsets) and kept as a pair for the corner values.
+ADECO_HD inline F2 face_value_at_cell(const WarpTets &W, const GridDesc &g, int s, int a, int b, int c, int f)
 {
     const int cc[3] = {a, b, c};
     F2 G = {-W.d[f][s], -W.dlo[f][s]};
@@ -599,7 +599,7 @@ ADECO_HD inline float face_value_at_cell(const WarpTets &W, const GridDesc &g, i
         G = f2_add(G, f2_two_prod(nx, fc));
         small = fmaf(nx * fc, g.drcell[x], small);
     }
-    return G.hi + (G.lo + small);
+    return f2_norm(G.hi, G.lo + small);
 }
 
 // 6x volume of cell (a, b, c) ∩ slot s's tet when the cell straddles only the
@@ -613,11 +613,11 @@ inline
 float facecut_pair_vol6(const WarpTets &W, const GridDesc &g, int s, int a, int b, int c, int cross)
 {
     const int f1 = cross & 3, f2 = (cross >> 2) - 1;
-    const float G1 = face_value_at_cell(W, g, s, a, b, c, f1);
-    if (f2 < 0) return halfspace_cube_vol6(G1, W.n[f1][0][s], W.n[f1][1][s], W.n[f1][2][s]);
-    const float G2 = face_value_at_cell(W, g, s, a, b, c, f2);
-    return twoplane_cube_vol6(G1, W.n[f1][0][s], W.n[f1][1][s], W.n[f1][2][s], G2, W.n[f2][0][s], W.n[f2][1][s],
-                              W.n[f2][2][s]);
+    float P1[8], P2[8];
+    cube_corner_values(face_value_at_cell(W, g, s, a, b, c, f1), W.n[f1][0][s], W.n[f1][1][s], W.n[f1][2][s], P1);
+    if (f2 < 0) return halfspace_cube_vol6(P1);
+    cube_corner_values(face_value_at_cell(W, g, s, a, b, c, f2), W.n[f2][0][s], W.n[f2][1][s], W.n[f2][2][s], P2);
+    return twoplane_cube_vol6(P1, P2);
 }
 
 // Non-negative mass of a pair (FP32, about 1e-7 relative) -> the cell's
