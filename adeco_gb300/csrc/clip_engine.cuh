@@ -244,84 +244,6 @@ ADECO_HD inline F2 f2_minor(F2 a, F2 d, F2 b, F2 c)
     return f2_add(f2_mul(a, d), {-bc.hi, -bc.lo});
 }
 
-// Inside fraction of a tet for a linear function with values b0..b3 at its
-// vertices (inside: > 0): 0, 1 or side_fraction's edge-parameter formula.
-ADECO_HD inline float plane_fraction(float b0, float b1, float b2, float b3)
-{
-    const int m = (int)(b0 > 0.f) | ((int)(b1 > 0.f) << 1) | ((int)(b2 > 0.f) << 2) | ((int)(b3 > 0.f) << 3);
-    return m == 15 ? 1.f : (m == 0 ? 0.f : side_fraction(b0, b1, b2, b3, m, 0.f));
-}
-
-// 6x volume of the unit cube's part where both G1 > 0 and G2 > 0, from their
-// values at the 8 corners (cube_corner_values) -- a cell that two tet faces
-// cut, inside the other two.  Each of the cube's 6 diagonal (Kuhn) tets, of 6x volume 1, is cut by
-// plane 1 into 1 or 3 sub-tets, split_piece's patterns over the inside-first
-// vertices A B C D (k inside):
-//   k = 1: (A, Xab, Xac, Xad)                          weight tAB tAC tAD
-//   k = 2: (A, B, Xbc, Xbd) (A, Xbc, Xac, Xbd) (A, Xac, Xad, Xbd)
-//          weights tBC tBD,  tAC uBC tBD,  tAC tAD uBD
-//   k = 3: (A, B, C, Xcd) (A, B, Xcd, Xbd) (A, Xbd, Xcd, Xad)
-//          weights tCD,  tBD uCD,  tAD uBD uCD
-// (each sub-tet's volume over the Kuhn tet's, from the edge parameters t of
-// plane 1 and u = 1 - t), and each sub-tet's part inside plane 2 comes from
-// plane 2's values at its vertices -- interpolated along the same edges -- by
-// plane_fraction.  Non-negative terms only: no cancellation, as for one face.
-ADECO_HD inline float twoplane_cube_vol6(const float P1[8], const float P2[8])
-{
-    const int path[6][2] = {{1, 3}, {1, 5}, {2, 3}, {2, 6}, {4, 5}, {4, 6}};
-    float v = 0.f;
-#pragma unroll
-    for (int q = 0; q < 6; ++q) {
-        const float a0 = P1[0], a1 = P1[path[q][0]], a2 = P1[path[q][1]], a3 = P1[7];
-        const float b0 = P2[0], b1 = P2[path[q][0]], b2 = P2[path[q][1]], b3 = P2[7];
-        const int m = (int)(a0 > 0.f) | ((int)(a1 > 0.f) << 1) | ((int)(a2 > 0.f) << 2) | ((int)(a3 > 0.f) << 3);
-        if (m == 0) continue;
-        if (m == 15) {
-            v += plane_fraction(b0, b1, b2, b3);
-            continue;
-        }
-        const int pm = split_perm(m), k = split_kin(m);
-        const float A = sel4(pm & 3, a0, a1, a2, a3), B = sel4((pm >> 2) & 3, a0, a1, a2, a3);
-        const float C = sel4((pm >> 4) & 3, a0, a1, a2, a3), D = sel4((pm >> 6) & 3, a0, a1, a2, a3);
-        const float bA = sel4(pm & 3, b0, b1, b2, b3), bB = sel4((pm >> 2) & 3, b0, b1, b2, b3);
-        const float bC = sel4((pm >> 4) & 3, b0, b1, b2, b3), bD = sel4((pm >> 6) & 3, b0, b1, b2, b3);
-        // edges as in side_fraction: k=1: AB AC AD; k=2: AC AD BC BD; k=3: AD BD CD
-        const float i0 = A, o0 = (k == 1) ? B : ((k == 2) ? C : D);
-        const float i1 = (k == 3) ? B : A, o1 = (k == 1) ? C : D;
-        const float i2 = (k == 1) ? A : ((k == 2) ? B : C), o2 = (k == 2) ? C : D;
-        const float i3 = B, o3 = D;
-        const float bi0 = bA, bo0 = (k == 1) ? bB : ((k == 2) ? bC : bD);
-        const float bi1 = (k == 3) ? bB : bA, bo1 = (k == 1) ? bC : bD;
-        const float bi2 = (k == 1) ? bA : ((k == 2) ? bB : bC), bo2 = (k == 2) ? bC : bD;
-        const float bi3 = bB, bo3 = bD;
-        const float in[4] = {i0, i1, i2, i3}, out[4] = {o0, o1, o2, o3};
-        float t[4], u[4];
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-#ifdef __CUDA_ARCH__
-            const float r = __frcp_rn(out[e] - in[e]);
-#else
-            const float r = 1.f / (out[e] - in[e]);
-#endif
-            t[e] = fminf(fmaxf(-in[e] * r, 0.f), 1.f);
-            u[e] = fminf(fmaxf(out[e] * r, 0.f), 1.f);
-        }
-        // plane 2 at the cut points of edges 0..3
-        const float x0 = fmaf(t[0], bo0 - bi0, bi0), x1 = fmaf(t[1], bo1 - bi1, bi1);
-        const float x2 = fmaf(t[2], bo2 - bi2, bi2), x3 = fmaf(t[3], bo3 - bi3, bi3);
-        if (k == 1) {  // E0=Xab E1=Xac E2=Xad
-            v += (t[0] * t[1] * t[2]) * plane_fraction(bA, x0, x1, x2);
-        } else if (k == 2) {  // E0=Xac E1=Xad E2=Xbc E3=Xbd
-            v += (t[2] * t[3]) * plane_fraction(bA, bB, x2, x3) + (t[0] * u[2] * t[3]) * plane_fraction(bA, x2, x0, x3) +
-                 (t[0] * t[1] * u[3]) * plane_fraction(bA, x0, x1, x3);
-        } else {  // E0=Xad E1=Xbd E2=Xcd
-            v += t[2] * plane_fraction(bA, bB, bC, x2) + (t[1] * u[2]) * plane_fraction(bA, bB, x2, x1) +
-                 (t[0] * u[1] * u[2]) * plane_fraction(bA, x1, x2, x0);
-        }
-    }
-    return v;
-}
-
 // ---------------------------------------------------- barycentric clipping// ---------------------------------------------------- barycentric clipping
 // Fraction of a tet's volume inside the unit cube, for tets too flat for the
 // FP32 engine.  A flat tet's volume L^2 h, computed from FP32 coordinates as

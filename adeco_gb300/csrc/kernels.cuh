@@ -537,9 +537,9 @@ int classify_fp64(const WarpTets &W, const GridDesc &g, int s, int a, int b, int
     return all_in ? P_CELL_INSIDE : P_PARTIAL;
 }
 
-// cross: the tet face planes the cell straddles when the cell is certainly
-// inside the others -- then cell ∩ tet = cell ∩ their half-spaces: one face f
-// (cross = f) or two faces f1 < f2 (cross = f1 + 4 (f2 + 1)); else -1.
+// cross: the one tet face plane the cell straddles when the cell is certainly
+// inside the other three (then cell ∩ tet = cell ∩ that face's half-space),
+// else -1.
 ADECO_HD inline int classify_pair(const WarpTets &W, const GridDesc &g, int s, int a, int b, int c, bool &used_fp64,
                                   int &cross)
 {
@@ -553,7 +553,7 @@ ADECO_HD inline int classify_pair(const WarpTets &W, const GridDesc &g, int s, i
         W.bmin[2][s] >= fc && W.bmax[2][s] <= fc + 1.f)
         return P_TET_INSIDE;
     bool all_in = true, unsure = false;
-    int ncross = 0, fcross = 0, ffirst = 0;
+    int ncross = 0, fcross = 0;
     const float t = W.tol[s];
 #pragma unroll
     for (int f = 0; f < 4; ++f) {
@@ -566,7 +566,6 @@ ADECO_HD inline int classify_pair(const WarpTets &W, const GridDesc &g, int s, i
         if (mx <= t) unsure = true;
         if (mn > t) continue;
         all_in = false;
-        if (ncross == 0) ffirst = f;
         ++ncross;
         fcross = f;
         if (mn > -t) unsure = true;
@@ -576,7 +575,6 @@ ADECO_HD inline int classify_pair(const WarpTets &W, const GridDesc &g, int s, i
         return classify_fp64(W, g, s, a, b, c);
     }
     if (ncross == 1) cross = fcross;
-    if (ncross == 2) cross = ffirst + 4 * (fcross + 1);
     return all_in ? P_CELL_INSIDE : P_PARTIAL;
 }
 
@@ -602,22 +600,18 @@ ADECO_HD inline F2 face_value_at_cell(const WarpTets &W, const GridDesc &g, int 
     return f2_norm(G.hi, G.lo + small);
 }
 
-// 6x volume of cell (a, b, c) ∩ slot s's tet when the cell straddles only the
-// face(s) `cross` names (classify_pair): one face, the cube's part on its
-// inside; two faces, the part inside both.
+// 6x volume of cell (a, b, c) ∩ slot s's tet when the cell straddles only
+// face f: the cube's part on its inside.
 #ifdef __CUDA_ARCH__
 __device__ __noinline__
 #else
 inline
 #endif
-float facecut_pair_vol6(const WarpTets &W, const GridDesc &g, int s, int a, int b, int c, int cross)
+float halfspace_pair_vol6(const WarpTets &W, const GridDesc &g, int s, int a, int b, int c, int f)
 {
-    const int f1 = cross & 3, f2 = (cross >> 2) - 1;
-    float P1[8], P2[8];
-    cube_corner_values(face_value_at_cell(W, g, s, a, b, c, f1), W.n[f1][0][s], W.n[f1][1][s], W.n[f1][2][s], P1);
-    if (f2 < 0) return halfspace_cube_vol6(P1);
-    cube_corner_values(face_value_at_cell(W, g, s, a, b, c, f2), W.n[f2][0][s], W.n[f2][1][s], W.n[f2][2][s], P2);
-    return twoplane_cube_vol6(P1, P2);
+    float P[8];
+    cube_corner_values(face_value_at_cell(W, g, s, a, b, c, f), W.n[f][0][s], W.n[f][1][s], W.n[f][2][s], P);
+    return halfspace_cube_vol6(P);
 }
 
 // Non-negative mass of a pair (FP32, about 1e-7 relative) -> the cell's
@@ -820,8 +814,8 @@ __device__ __forceinline__ void pair_range(const DepositParams &P, const GridDes
             } else if (cls == P_PARTIAL) {
                 ++st.part;
                 ++st.bbox;
-                if (cross >= 0) {  // one or two faces cut the cell: closed form, no clipping
-                    const float dm = facecut_pair_vol6(Wc, g, s, a, b, c, cross) * Wc.f6[s];
+                if (cross >= 0) {  // one face cuts the cell: closed form, no clipping
+                    const float dm = halfspace_pair_vol6(Wc, g, s, a, b, c, cross) * Wc.f6[s];
                     if (dm > 0.f) scatter(P, g, Wc, s, a, b, c, dm);
                 } else {
                     part = true;

@@ -59,8 +59,8 @@ int main()
     static WarpTets W;
     const double cell_sizes[4] = {0.25, 0.5, 1.0, 2.0};
     double worst_rel = 0.0, worst_abs = 0.0, sum_err = 0.0, sum_mass = 0.0;
-    double wr[4] = {0, 0, 0, 0}, wa[4] = {0, 0, 0, 0};  // by path: 0 exact classes, 1 one-face closed form, 2 clipped, 3 two-face closed form
-    long npath[4] = {0, 0, 0, 0};
+    double wr[3] = {0, 0, 0}, wa[3] = {0, 0, 0};  // by path: 0 exact classes, 1 one-face closed form, 2 clipped
+    long npath[3] = {0, 0, 0};
     long pairs = 0, partial = 0, tets = 0;
     for (int trial = 0; trial < 4000; ++trial) {
         const double dx = cell_sizes[trial % 4];
@@ -113,8 +113,8 @@ int main()
                         } else if (cls == P_PARTIAL) {
                             // the GPU's FP32 pair masses (then converted to fixed point exactly)
                             if (cross >= 0) {
-                                dm = (double)(facecut_pair_vol6(W, g, 0, a, b, c, cross) * W.f6[0]);
-                                path = cross < 4 ? 1 : 3;
+                                dm = (double)(halfspace_pair_vol6(W, g, 0, a, b, c, cross) * W.f6[0]);
+                                path = 1;
                             } else {
                                 path = 2;
                                 float p[12];
@@ -144,16 +144,14 @@ int main()
     std::printf("tets %ld, pairs %ld (%ld clipped): worst relative error %.3e (pairs above 1e-3 tet masses), "
                 "worst absolute %.3e tet masses, summed error %.3e of %.1f\n",
                 tets, pairs, partial, worst_rel, worst_abs, sum_err, sum_mass);
-    const char *names[4] = {"inside / holding", "one-face closed form", "clipped", "two-face closed form"};
-    for (int k = 0; k < 4; ++k)
+    const char *names[3] = {"inside / holding", "one-face closed form", "clipped"};
+    for (int k = 0; k < 3; ++k)
         std::printf("  %s (%ld pairs): worst relative %.3e, worst absolute %.3e\n", names[k], npath[k], wr[k], wa[k]);
     // Bounds, per pair: the clip engine's FP32 steps (worst 1.4e-5 relative on pairs above 1e-3 tet
     // masses, 6.7e-7 absolute: slices under an upper face of tets that also cross the lower face);
     // the closed form (3.7e-6, 3.7e-8).  Summed over all pairs the error must stay below 6e-10 of the
     // mass: 3.7e-10 with the mirrored frames of piece_coords, 1.0e-9 without them.
-    // The two-face closed form (cells cut by two tet faces): 1.4e-5 relative, 3.1e-7 absolute, as the engine.
     const bool ok = wr[2] < 5e-5 && wa[2] < 2e-6 && wr[1] < 2e-5 && wa[1] < 2e-7 && wr[0] < 1e-6 && wa[0] < 1e-6 &&
-                    wr[3] < 5e-5 && wa[3] < 2e-6 && npath[3] > 0 &&
                     std::fabs(sum_err) < 6e-10 * sum_mass;
     std::printf("%s\n", ok ? "ok" : "FAIL");
     return ok ? 0 : 1;
