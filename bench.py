@@ -194,14 +194,16 @@ def measured_peaks():
         return {}
 
 
-def profile_traffic():
-    """DRAM bytes per launch of the deposit kernel from the committed ncu summary."""
+def profile_figure(name):
+    """A per-launch figure of the deposit kernel (`name: value`) from the
+    committed ncu summary: dram_bytes_per_launch_full_workload (DRAM read +
+    write), fp32_flops_per_launch_full_workload (executed FADD + FMUL + 2 FFMA)."""
     path = os.path.join(ROOT, "profiles", "deposit_mixed_kernel_c2.md")
     try:
         text = open(path).read()
     except OSError:
         return None
-    m = re.search(r"dram_bytes_per_launch_full_workload:\s*([0-9.eE+]+)", text)
+    m = re.search(name + r":\s*([0-9.eE+]+)", text)
     return float(m.group(1)) if m else None
 
 
@@ -438,12 +440,18 @@ def run_ours(args, rank, ws, local):
     hbm = peaks.get("hbm_gbs")
     # the committed ncu summary covers the default 256^3 workload only
     c2 = (N_PART, SEED, INFALL, MAX_LEVEL) == (256, 0, 0, 8)
-    traffic = profile_traffic() if c2 else None
+    traffic = profile_figure("dram_bytes_per_launch_full_workload") if c2 else None
+    exec_flops = profile_figure("fp32_flops_per_launch_full_workload") if c2 else None
     roof = {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s", "frac": achieved / peak.value,
             "traffic": traffic, "peak_source": "measured FP32 FMA probe (adeco_probe_fp32_tflops) on this GPU",
             "flops_per_launch": alg_flops, "flops_model": "reference-algorithm FLOPs counted by the instrumented "
             "oracle on a spread sample of leaves, per meta-cell tet, x all leaves' meta-cell tets",
             "kernel_ms": out["kernel_ms"],
+            # the FP32 operations the kernel executes (ncu, scaled to this workload) over the same time
+            "executed_fp32": None if exec_flops is None else {
+                "flops_per_launch": exec_flops, "achieved_tflops": exec_flops / k_s / 1e12,
+                "frac": exec_flops / k_s / 1e12 / peak.value,
+                "source": "ncu smsp__sass_thread_inst_executed_op_{fadd,fmul,ffma}_pred_on (FFMA x2), profiles/"},
             "hbm": {"achieved_gbs": alg_bytes / k_s / 1e9, "peak_gbs": hbm, "frac_of_measured":
                     (alg_bytes / k_s / 1e9 / hbm) if hbm else None, "algorithmic_bytes": alg_bytes}}
     # CPU baseline: the oracle (reference algorithm, FP32) on a bounded sample
