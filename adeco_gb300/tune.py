@@ -39,8 +39,8 @@ SPACES = {
     # octree leaf blocks (coarse grids: a tet meets a few cells)
     "leaf": {"clip_batch": [64, 96, 128], "ctas_per_sm": [1, 2]},
     # zoom grids (fine grids: cells much smaller than tets)
-    "zoom": {"zoom_tile": [32, 48, 64, 96, 128], "item_pairs": [1 << 16, 1 << 17, 1 << 18, 1 << 20],
-             "share_chunk": [256, 512, 1024, 2048], "clip_batch": [64, 96, 128]},
+    "zoom": {"zoom_tile": [32, 64, 128], "item_pairs": [1 << 16, 1 << 17, 1 << 18, 1 << 20],
+             "share_chunk": [256, 512, 1024], "clip_batch": [96, 128]},
 }
 DEFAULTS = {"zoom_tile": 64, "share_chunk": 512, "clip_batch": 128, "ctas_per_sm": 2, "item_pairs": 1 << 18}
 
@@ -152,7 +152,10 @@ def tune_leaves(session, workload, reps=3, cache=None, device=0, force=False, lo
 
 def tune_zoom(session, requests, workload, reps=1, cache=None, device=0, force=False, log=None):
     """Tunes zoom batches on a sample batch `requests`: each trial is the
-    device time of the batch (median of `reps`).  Returns (params, info)."""
+    device time of the batch (median of `reps`).  The sample must load the GPU
+    like the batches to be served: a batch of 64 of the 512 zoom requests
+    picked a tile and item size 15% slower on the whole batch than the
+    defaults.  Returns (params, info)."""
     cache = cache or TuneCache()
     key = TuneCache.key(gpu_id(device), "zoom", workload)
     hit = None if force else cache.get(key)

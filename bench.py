@@ -472,7 +472,7 @@ def run_ours(args, rank, ws, local):
                    "precision": "FP32 clipping in mirrored cell frames (kappa>32 tets: barycentric, double-float shares); "
                                 "FP64 near-degenerate classification and volume normalisers; "
                                 "64-bit fixed-point accumulation",
-                   "l2": "inputs larger than L2 (268 MB float4 lattice); no flush", "cuda_graph": True,
+                   "l2": f"inputs larger than L2 ({16 * n ** 3 / 1e6:.0f} MB float4 lattice); no flush", "cuda_graph": True,
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "roofline": roof,
         "cpu_baseline": cpu,
@@ -579,8 +579,9 @@ def serve_leg(args, pos, rate=None):
 
 
 def zoom_leg(args, pos):
-    """512 zoom requests (C3) in one batch: autotuned tile / chunk / staging
-    depth on a 64-request sample, then whole batches timed on the device."""
+    """512 zoom requests (C3) in one batch: autotuned tile / item size / chunk /
+    staging depth on every other request, then whole batches timed on the
+    device."""
     from adeco_gb300 import deposit as D
     from adeco_gb300 import tune
     from adeco_gb300.synthetic import zoom_requests
@@ -590,7 +591,7 @@ def zoom_leg(args, pos):
         if args.no_tune:
             params, tinfo = s.get_tuning(), {"source": "defaults"}
         else:
-            params, tinfo = tune.tune_zoom(s, reqs[:64], f"{len(reqs)} zoom requests, seed {ZOOM_SEED}",
+            params, tinfo = tune.tune_zoom(s, reqs[::2], f"{len(reqs)} zoom requests, seed {ZOOM_SEED}",
                                            device=args.device, force=args.retune)
         ms = []
         for k in range(1 + args.zoom_steps):
