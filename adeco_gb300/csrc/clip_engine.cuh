@@ -198,73 +198,6 @@ ADECO_HD inline float inside_fraction(const float p[12], int mask, int f)
     return side_fraction(x0, x1, x2, x3, mask, (f & 1) ? 1.f : 0.f);
 }
 
-// Fraction of piece p inside both of the last two cell faces it crosses, f1 <
-// f2 (mask1: its vertices inside f1), in one step: the split by f1 is not
-// built.  Its 1 or 3 sub-tets (split_piece's patterns over the inside-first
-// vertices A B C D, k inside f1) have these shares of the piece, from f1's
-// edge parameters t and u = 1 - t:
-//   k = 1: (A, Xab, Xac, Xad)                           tAB tAC tAD
-//   k = 2: (A, B, Xbc, Xbd) (A, Xbc, Xac, Xbd) (A, Xac, Xad, Xbd)
-//          tBC tBD,  tAC uBC tBD,  tAC tAD uBD
-//   k = 3: (A, B, C, Xcd) (A, B, Xcd, Xbd) (A, Xbd, Xcd, Xad)
-//          tCD,  tBD uCD,  tAD uBD uCD
-// and each sub-tet's fraction inside f2 comes from its vertices' coordinates
-// along f2's axis (the cut points' interpolated along the same edges) by
-// side_fraction.  Non-negative terms only, as the last-face fraction; it
-// replaces a split, its 1 or 3 pushed or kept children and their last-face
-// steps.
-ADECO_HD inline float twoface_fraction(const float p[12], int mask1, int f1, int f2)
-{
-    const int a1 = f1 >> 1, a2 = f2 >> 1;
-    const float pl1 = (f1 & 1) ? 1.f : 0.f, pl2 = (f2 & 1) ? 1.f : 0.f;
-    const float y0 = sel3(a1, p[0], p[1], p[2]), y1 = sel3(a1, p[3], p[4], p[5]);
-    const float y2 = sel3(a1, p[6], p[7], p[8]), y3 = sel3(a1, p[9], p[10], p[11]);
-    const float z0 = sel3(a2, p[0], p[1], p[2]), z1 = sel3(a2, p[3], p[4], p[5]);
-    const float z2 = sel3(a2, p[6], p[7], p[8]), z3 = sel3(a2, p[9], p[10], p[11]);
-    const int pm = split_perm(mask1), k = split_kin(mask1);
-    const int ia = pm & 3, ib = (pm >> 2) & 3, ic = (pm >> 4) & 3, id = (pm >> 6) & 3;
-    const float A = sel4(ia, y0, y1, y2, y3), B = sel4(ib, y0, y1, y2, y3);
-    const float C = sel4(ic, y0, y1, y2, y3), D = sel4(id, y0, y1, y2, y3);
-    const float zA = sel4(ia, z0, z1, z2, z3), zB = sel4(ib, z0, z1, z2, z3);
-    const float zC = sel4(ic, z0, z1, z2, z3), zD = sel4(id, z0, z1, z2, z3);
-    // edges as in side_fraction: k=1: AB AC AD; k=2: AC AD BC BD; k=3: AD BD CD
-    const float in[4] = {A, (k == 3) ? B : A, (k == 1) ? A : ((k == 2) ? B : C), B};
-    const float out[4] = {(k == 1) ? B : ((k == 2) ? C : D), (k == 1) ? C : D, (k == 2) ? C : D, D};
-    const float zin[4] = {zA, (k == 3) ? zB : zA, (k == 1) ? zA : ((k == 2) ? zB : zC), zB};
-    const float zout[4] = {(k == 1) ? zB : ((k == 2) ? zC : zD), (k == 1) ? zC : zD, (k == 2) ? zC : zD, zD};
-    float t[4], u[4], X[4];
-#pragma unroll
-    for (int e = 0; e < 4; ++e) {
-#ifdef __CUDA_ARCH__
-        const float r = __frcp_rn(out[e] - in[e]);
-#else
-        const float r = 1.f / (out[e] - in[e]);
-#endif
-        t[e] = fminf(fmaxf((pl1 - in[e]) * r, 0.f), 1.f);
-        u[e] = fminf(fmaxf((out[e] - pl1) * r, 0.f), 1.f);
-        X[e] = fmaf(t[e], zout[e] - zin[e], zin[e]);  // the cut point's coordinate along f2's axis
-    }
-    const bool k1 = (k == 1), k2 = (k == 2);
-    const int nsub = k1 ? 1 : 3;
-    float v = 0.f;
-#pragma unroll 1
-    for (int j = 0; j < nsub; ++j) {
-        // sub-tet j: its vertices along f2's axis and its share of the piece
-        const float s0 = zA;
-        const float s1 = k1 ? X[0] : ((j == 2) ? (k2 ? X[0] : X[1]) : ((j == 1) ? (k2 ? X[2] : zB) : zB));
-        const float s2 = k1 ? X[1] : ((j == 0) ? (k2 ? X[2] : zC) : ((j == 1) ? (k2 ? X[0] : X[2]) : (k2 ? X[1] : X[2])));
-        const float s3 = k1 ? X[2] : ((j == 0) ? (k2 ? X[3] : X[2]) : ((j == 1) ? (k2 ? X[3] : X[1]) : (k2 ? X[3] : X[0])));
-        const float w = k1 ? t[0] * t[1] * t[2]
-                           : ((j == 0) ? (k2 ? t[2] * t[3] : t[2])
-                                       : ((j == 1) ? (k2 ? t[0] * u[2] * t[3] : t[1] * u[2])
-                                                   : (k2 ? t[0] * t[1] * u[3] : t[0] * u[1] * u[2])));
-        const int m2 = (f2 & 1) ? ((int)(s0 < 1.f) | ((int)(s1 < 1.f) << 1) | ((int)(s2 < 1.f) << 2) | ((int)(s3 < 1.f) << 3))
-                                : ((int)(s0 > 0.f) | ((int)(s1 > 0.f) << 1) | ((int)(s2 > 0.f) << 2) | ((int)(s3 > 0.f) << 3));
-        v += w * ((m2 == 15) ? 1.f : ((m2 == 0) ? 0.f : side_fraction(s0, s1, s2, s3, m2, pl2)));
-    }
-    return v;
-}
-
 // Values of a linear function G(u) = G0 + n.u at the unit cube's 8 corners
 // (k: bit 0 x, bit 1 y, bit 2 z) from G0 as a double-float pair: each corner
 // value is formed exactly (TwoSum) and rounded once, so that a value near
@@ -446,9 +379,7 @@ ADECO_HD inline float piece_vol6(const float p[12])
 
 // state of one piece: next face to examine -> (code, face); code 0 = dropped,
 // 1 = finished, 2 = split at `face` with inside mask `mask`
-// face2 (when given): the second crossed face when exactly two remain, else -1
-ADECO_HD inline int piece_step(const float p[12], int face0, int &face, int &mask, bool *last = nullptr,
-                               int *face2 = nullptr)
+ADECO_HD inline int piece_step(const float p[12], int face0, int &face, int &mask, bool *last = nullptr)
 {
     const int b0 = face_bits(p[0], p[1], p[2]), b1 = face_bits(p[3], p[4], p[5]);
     const int b2 = face_bits(p[6], p[7], p[8]), b3 = face_bits(p[9], p[10], p[11]);
@@ -464,20 +395,12 @@ ADECO_HD inline int piece_step(const float p[12], int face0, int &face, int &mas
 #endif
     mask = ((b0 >> face) & 1) | (((b1 >> face) & 1) << 1) | (((b2 >> face) & 1) << 2) | (((b3 >> face) & 1) << 3);
     if (last) *last = (next >> (face + 1)) == 0;
-    if (face2) {
-        const int rest = next & ~(1 << face);
-#ifdef __CUDA_ARCH__
-        *face2 = (rest && !(rest & (rest - 1))) ? __ffs(rest) - 1 : -1;
-#else
-        *face2 = (rest && !(rest & (rest - 1))) ? __builtin_ctz(rest) : -1;
-#endif
-    }
     return 2;
 }
 
 // Serial clipping of one piece from face `face0` on (used when the warp pool
-// is full): depth-first over the same splits and last-face / last-two-face
-// fractions, so the fixed-point sum is the warp engine's.
+// is full): depth-first over the same splits and last-face fractions, so the
+// fixed-point sum is the warp engine's.
 #ifdef __CUDA_ARCH__
 __device__ __noinline__
 #else
@@ -498,14 +421,12 @@ long long clip_piece_serial(const float p0[12], int face0)
         float p[12];
 #pragma unroll
         for (int x = 0; x < 12; ++x) p[x] = stk[sp][x];
-        int face = 0, mask = 0, face2 = -1;
+        int face = 0, mask = 0;
         bool last = false;
-        const int code = piece_step(p, sface[sp], face, mask, &last, &face2);
+        const int code = piece_step(p, sface[sp], face, mask, &last);
         if (code == 0) continue;
-        if (code == 1 || last || face2 >= 0) {
-            acc += vol_fixed(piece_vol6(p) * (code == 1 ? 1.f
-                                                        : (face2 >= 0 ? twoface_fraction(p, mask, face, face2)
-                                                                      : inside_fraction(p, mask, face))));
+        if (code == 1 || last) {
+            acc += vol_fixed(piece_vol6(p) * (code == 1 ? 1.f : inside_fraction(p, mask, face)));
             continue;
         }
         float c0[12], c1[12], c2[12];
@@ -600,10 +521,10 @@ __device__ __forceinline__ void clip_pairs(WarpPool &pool, int np, Build build, 
         // and none can move does one lane clip its piece alone (serially, with
         // a local stack): letting every pushing lane of a full pool do that
         // had put most of the fine-grid time into one-lane serial clipping.
-        int f = 0, mask = 0, code = 0, f2 = -1;
+        int f = 0, mask = 0, code = 0;
         bool last = false;
-        if (valid) code = piece_step(p, face, f, mask, &last, &f2);
-        const bool split = valid && code == 2 && !last && f2 < 0;
+        if (valid) code = piece_step(p, face, f, mask, &last);
+        const bool split = valid && code == 2 && !last;
         const int want = (split && split_kin(mask) != 1) ? 2 : 0;  // children to push
         int incl = want;
 #pragma unroll
@@ -635,12 +556,9 @@ __device__ __forceinline__ void clip_pairs(WarpPool &pool, int np, Build build, 
                     pool.meta[base + 1] = m;
                 }
             } else {
-                // finished, or at its last one or two crossed faces: the
-                // inside part needs no more clipping, so its volume is added here
-                if (code != 0)
-                    v = vol_fixed(piece_vol6(p) * (code == 1 ? 1.f
-                                                             : (f2 >= 0 ? twoface_fraction(p, mask, f, f2)
-                                                                        : inside_fraction(p, mask, f))));
+                // finished, or at its last crossed face: the inside part
+                // needs no more clipping, so its volume is added here
+                if (code != 0) v = vol_fixed(piece_vol6(p) * (code == 1 ? 1.f : inside_fraction(p, mask, f)));
                 valid = false;
             }
             if (v) atomicAdd(reinterpret_cast<unsigned long long *>(&pool.vacc[owner]), (unsigned long long)v);
