@@ -61,19 +61,38 @@ def dist_env():
 
 class Dist:
     """Barrier / max / sum over ranks (torch.distributed) for N > 1: NCCL on the
-    GPUs, or gloo with CPU tensors (the multi-rank logic tested without a GPU)."""
+    GPUs, or gloo with CPU tensors (the multi-rank logic tested without a GPU).
+    Collectives and the rendezvous give up after `timeout_s` (default from
+    ADECO_PG_TIMEOUT_S, else 600 s), so a rank that never joins ends the others'
+    wait with an error instead of a hang."""
 
-    def __init__(self, ws, local, backend="nccl"):
+    def __init__(self, ws, local, backend="nccl", timeout_s=None):
         self.ws = ws
         self.pg = None
         if ws > 1:
+            import datetime
+
             import torch
             import torch.distributed as dist
             if backend == "nccl":
                 torch.cuda.set_device(local)
-            dist.init_process_group(backend)
+            if timeout_s is None:
+                timeout_s = float(os.environ.get("ADECO_PG_TIMEOUT_S", "600"))
+            dist.init_process_group(backend, timeout=datetime.timedelta(seconds=timeout_s))
             self.torch, self.dist = torch, dist
             self.device = "cuda" if backend == "nccl" else "cpu"
+
+    def agree(self, ok):
+        """True when every rank reports ok.  A rank whose host work failed
+        reports False before it leaves; a rank that died, or never reaches this
+        point within the timeout, makes the collective fail, which counts as
+        False here."""
+        if self.ws == 1:
+            return bool(ok)
+        try:
+            return self._reduce(1.0 if ok else 0.0, self.dist.ReduceOp.MIN) == 1.0
+        except Exception:  # noqa: BLE001 -- a peer that is gone or timed out
+            return False
 
     def barrier(self):
         if self.ws > 1:
@@ -93,6 +112,26 @@ class Dist:
     def close(self):
         if self.ws > 1:
             self.dist.destroy_process_group()
+
+
+class RankFailure(RuntimeError):
+    """Another rank failed before the timed region; no number is reported."""
+
+
+def gated(dist, fn, what):
+    """Runs this rank's untimed work fn(), then has all ranks agree that each
+    got through its own before any rank enters the timed region (a rank leaves
+    only here, between steps, with no kernel or collective of its own in
+    flight).  The failing rank re-raises its own error; the others raise
+    RankFailure."""
+    try:
+        r = fn()
+    except BaseException:
+        dist.agree(False)
+        raise
+    if not dist.agree(True):
+        raise RankFailure(f"another rank failed during {what}; no number is reported")
+    return r
 
 
 def replica_value(dist, tets, ms):
@@ -322,23 +361,27 @@ def run_ours(args, rank, ws, local):
     tets = 6 * (n - 1) ** 3
     out = {}
     with D.Session(pos, device=local if ws > 1 else args.device) as s:
-        info = s.build_octree(MAX_TETS, MAX_LEVEL, leaf_dims=LEAF)
+        def setup():
+            info = s.build_octree(MAX_TETS, MAX_LEVEL, leaf_dims=LEAF)
+            out["gpu_tree"] = (info, [s.leaf_meta(q) for q in range(len(info.leaves))])
+            # launch shape and staging depth: picked by the autotuner for this GPU and workload
+            if not args.no_tune:
+                from adeco_gb300 import tune
+                params, tinfo = tune.tune_leaves(s, WORKLOAD, device=local if ws > 1 else args.device,
+                                                 force=args.retune)
+                out["tuning"] = {"leaf": params, **{k: v for k, v in tinfo.items() if k != "key"}}
+            else:
+                out["tuning"] = {"leaf": s.get_tuning(), "source": "defaults"}
+            # one untimed pass with the pair counters on
+            grids, st = s.deposit_leaves(stats=True)
+            for _ in range(args.warmup):
+                s.replay_leaves(1)
+            kern = [s.deposit_leaves(fetch=False)[1]["kernel_ms"] for _ in range(2)]
+            return info, grids, st, kern
+
+        info, grids, st, kern = gated(dist, setup, "the octree build and warm-up")
         nleaf = len(info.leaves)
-        out["gpu_tree"] = (info, [s.leaf_meta(q) for q in range(nleaf)])
-        # launch shape and staging depth: picked by the autotuner for this GPU and workload
-        if not args.no_tune:
-            from adeco_gb300 import tune
-            params, tinfo = tune.tune_leaves(s, WORKLOAD, device=local if ws > 1 else args.device,
-                                             force=args.retune)
-            out["tuning"] = {"leaf": params, **{k: v for k, v in tinfo.items() if k != "key"}}
-        else:
-            out["tuning"] = {"leaf": s.get_tuning(), "source": "defaults"}
-        # one untimed pass with the pair counters on
-        grids, st = s.deposit_leaves(stats=True)
         mixed_total = float(grids.sum())
-        for _ in range(args.warmup):
-            s.replay_leaves(1)
-        kern = [s.deposit_leaves(fetch=False)[1]["kernel_ms"] for _ in range(2)]
         dist.barrier()
         with ClockSampler(local if ws > 1 else args.device) as clk:
             t = s.replay_leaves(args.steps)
