@@ -8,8 +8,9 @@
 //     64-bit fixed point, to the accumulator of the pair it came from, or
 //   * at the last cell face it crosses, adds the inside fraction of its
 //     volume (from the edge parameters alone, no cut points), or
-//   * splits it by the next cell face it crosses into 1 or 3 inside pieces,
-//     keeps one and pushes the others onto a per-warp shared-memory pool;
+//   * splits it by a cell face it crosses (of those, one with the fewest of
+//     its vertices inside: next_face) into 1 or 3 inside pieces, keeps one
+//     and pushes the others onto a per-warp shared-memory pool;
 // then idle lanes pop pieces from the pool (last in, first out).  All lanes
 // run the same split code every step, so a pair whose tet crosses several
 // faces (up to 3^6 pieces) spreads over the warp instead of serialising one
@@ -62,16 +63,33 @@ ADECO_HD inline int face_bits(float x, float y, float z)
            ((int)(z > 0.f) << 4) | ((int)(z < 1.f) << 5);
 }
 
+// 1/d with round-to-nearest errors only: the hardware's approximate
+// reciprocal (PTX rcp.approx) refined by one Newton-Raphson step, r + r (1 -
+// d r) in fused multiply-adds.  Measured on GB300 over d log-uniform in
+// [2^-8, 2^4]: the approximate reciprocal's mean signed relative error is
+// +3.7e-9 (it errs the same way for most d), the refined one's 3.4e-12, the
+// same as the correctly rounded reciprocal's.  Through the edge parameters of
+// every cut point and last-face fraction the approximate one showed as a
+// total-mass excess of 4e-9 relative on a 96^3 lattice.  For the engine's
+// denominators: differences of cell-frame coordinates across a face, nonzero
+// and far from the float range limits.
+ADECO_HD inline float rcp_nr(float d)
+{
+#ifdef __CUDA_ARCH__
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(d));
+    return fmaf(r, fmaf(-d, r, 1.f), r);
+#else
+    return 1.f / d;
+#endif
+}
+
 // point where edge in->out crosses the plane x_axis = plane (snapped onto it)
 ADECO_HD inline void cut_point(const float *pin, const float *pout, int axis, float plane, float *x)
 {
     const float din = sel3(axis, pin[0], pin[1], pin[2]);
     const float dout = sel3(axis, pout[0], pout[1], pout[2]);
-#ifdef __CUDA_ARCH__
-    float t = __fdividef(plane - din, dout - din);  // |dout - din| > 0 for a crossing edge
-#else
-    float t = (plane - din) / (dout - din);
-#endif
+    float t = (plane - din) * rcp_nr(dout - din);  // |dout - din| > 0 for a crossing edge
     t = fminf(fmaxf(t, 0.f), 1.f);
     x[0] = (axis == 0) ? plane : fmaf(t, pout[0] - pin[0], pin[0]);
     x[1] = (axis == 1) ? plane : fmaf(t, pout[1] - pin[1], pin[1]);
@@ -175,13 +193,9 @@ ADECO_HD inline float side_fraction(float x0, float x1, float x2, float x3, int 
     const float in[4] = {i0, i1, i2, i3}, out[4] = {o0, o1, o2, o3};
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
-        // round-to-nearest reciprocal: an approximate one biases the
+        // an unbiased reciprocal (rcp_nr): an approximate one biases the
         // fractions of all pairs the same way and shows in the total mass
-#ifdef __CUDA_ARCH__
-        const float r = __frcp_rn(out[e] - in[e]);
-#else
-        const float r = 1.f / (out[e] - in[e]);
-#endif
+        const float r = rcp_nr(out[e] - in[e]);
         t[e] = fminf(fmaxf((plane - in[e]) * r, 0.f), 1.f);
         u[e] = fminf(fmaxf((out[e] - plane) * r, 0.f), 1.f);
     }
@@ -244,7 +258,41 @@ ADECO_HD inline F2 f2_minor(F2 a, F2 d, F2 b, F2 c)
     return f2_add(f2_mul(a, d), {-bc.hi, -bc.lo});
 }
 
-// ---------------------------------------------------- barycentric clipping// ---------------------------------------------------- barycentric clipping
+// The cell face a piece is clipped by next, from its vertices' 6-bit inside
+// flags b0..b3 and the faces already done (`done`, one bit per face):
+// returns 0 if the piece lies beyond a remaining face (dropped), 1 if it lies
+// inside all of them (finished), else 2 with `face` the crossed face that has
+// the fewest of the piece's vertices inside, `mask` those vertices and `last`
+// set when no other face is crossed.  Fewest inside first: a single inside
+// vertex gives a single child, the corner tet at that vertex, which often
+// clears the other faces; two or three give three children.  Serial model on
+// lattice-like tets, steps per clipped pair with the lowest crossed face
+// first / this order: 19.1 / 8.7 at cells half a tet wide, 8.5 / 5.2 at
+// tet-sized cells, 4.2 / 3.1 at cells two tets wide.
+ADECO_HD inline int next_face(int b0, int b1, int b2, int b3, int done, int &face, int &mask, bool &last)
+{
+    const int all_in = b0 & b1 & b2 & b3, any_in = b0 | b1 | b2 | b3;
+    const int relevant = 63 & ~done;
+    if ((~any_in) & relevant) return 0;  // entirely outside a remaining face
+    const int next = (~all_in) & relevant;
+    if (!next) return 1;
+    // per crossed face 1..3 vertices inside: odd -> 1 or 3, `two` -> at least 2
+    const int odd = b0 ^ b1 ^ b2 ^ b3;
+    const int two = (b0 & b1) | (b2 & b3) | ((b0 | b1) & (b2 | b3));
+    int pick = next & odd & ~two;   // one vertex inside
+    if (!pick) pick = next & ~odd;  // two inside
+    if (!pick) pick = next;         // three inside
+#ifdef __CUDA_ARCH__
+    face = __ffs(pick) - 1;
+#else
+    face = __builtin_ctz(pick);
+#endif
+    mask = ((b0 >> face) & 1) | (((b1 >> face) & 1) << 1) | (((b2 >> face) & 1) << 2) | (((b3 >> face) & 1) << 3);
+    last = (next & (next - 1)) == 0;
+    return 2;
+}
+
+// ---------------------------------------------------- barycentric clipping
 // Fraction of a tet's volume inside the unit cube, for tets too flat for the
 // FP32 engine.  A flat tet's volume L^2 h, computed from FP32 coordinates as
 // a determinant, carries an error ~ 2^-24 L^3 -- relative 2^-24 kappa.  Here
@@ -278,21 +326,21 @@ ADECO_HD inline F2 bary_share(const float *w)
 constexpr int kBaryRec = 28;  // a barycentric piece: 16 weights (4 per vertex), then 12 coordinates
 
 // The share inside the unit cube of one barycentric piece rec0 whose faces
-// below face0 are already done, clipped serially with a stack.
+// in done0 are already done, clipped serially with a stack.
 ADECO_HD
 #ifdef __CUDA_ARCH__
 __noinline__
 #else
 inline
 #endif
-F2 clip_bary_serial(const float *rec0, int face0_in)
+F2 clip_bary_serial(const float *rec0, int done0)
 {
     constexpr int kDepth = 16;
     constexpr int kRec = kBaryRec;
     float stk[kDepth][kRec];
-    int sface[kDepth];
+    int sdone[kDepth];
     for (int i = 0; i < kRec; ++i) stk[0][i] = rec0[i];
-    sface[0] = face0_in;
+    sdone[0] = done0;
     int sp = 1;
     F2 acc = {0.f, 0.f};
     while (sp > 0) {
@@ -301,27 +349,20 @@ F2 clip_bary_serial(const float *rec0, int face0_in)
 #pragma unroll
         for (int i = 0; i < kRec; ++i) r[i] = stk[sp][i];
         const float *w = r, *x = r + 16;
-        const int face0 = sface[sp];
-        const int b0 = face_bits(x[0], x[1], x[2]), b1 = face_bits(x[3], x[4], x[5]);
-        const int b2 = face_bits(x[6], x[7], x[8]), b3 = face_bits(x[9], x[10], x[11]);
-        const int all_in = b0 & b1 & b2 & b3, any_in = b0 | b1 | b2 | b3;
-        const int relevant = (63 >> face0) << face0;
-        if ((~any_in) & relevant) continue;  // beyond a face
-        const int next = (~all_in) & relevant;
-        if (!next) {
+        const int done = sdone[sp];
+        int f = 0, mask = 0;
+        bool last = false;
+        const int code = next_face(face_bits(x[0], x[1], x[2]), face_bits(x[3], x[4], x[5]),
+                                   face_bits(x[6], x[7], x[8]), face_bits(x[9], x[10], x[11]), done, f, mask, last);
+        if (code == 0) continue;  // beyond a face
+        if (code == 1) {
             acc = f2_add(acc, bary_share(w));
             continue;
         }
-#ifdef __CUDA_ARCH__
-        const int f = __ffs(next) - 1;
-#else
-        const int f = __builtin_ctz(next);
-#endif
         const int axis = f >> 1;
         const float plane = (f & 1) ? 1.f : 0.f;
-        const int mask = ((b0 >> f) & 1) | (((b1 >> f) & 1) << 1) | (((b2 >> f) & 1) << 2) | (((b3 >> f) & 1) << 3);
         const float xa[4] = {x[axis], x[3 + axis], x[6 + axis], x[9 + axis]};
-        if ((next >> (f + 1)) == 0) {  // last crossed face: the inside fraction of the piece
+        if (last) {  // last crossed face: the inside fraction of the piece
             acc = f2_add(acc, f2_mul_f(bary_share(w), side_fraction(xa[0], xa[1], xa[2], xa[3], mask, plane)));
             continue;
         }
@@ -356,7 +397,7 @@ F2 clip_bary_serial(const float *rec0, int face0_in)
 #pragma unroll
                 for (int a = 0; a < 3; ++a) stk[sp][16 + 3 * v + a] = (src < 4) ? x[3 * id[src] + a] : E[src - 4][4 + a];
             }
-            sface[sp] = f + 1;
+            sdone[sp] = done | (1 << f);
             ++sp;
         }
     }
@@ -377,43 +418,30 @@ ADECO_HD inline float piece_vol6(const float p[12])
     return vol6_fast<float>(p, p + 3, p + 6, p + 9);
 }
 
-// state of one piece: next face to examine -> (code, face); code 0 = dropped,
-// 1 = finished, 2 = split at `face` with inside mask `mask`
-ADECO_HD inline int piece_step(const float p[12], int face0, int &face, int &mask, bool *last = nullptr)
+// state of one piece whose faces in `done` are done (next_face): code 0 =
+// dropped, 1 = finished, 2 = crossing `face` with inside mask `mask`
+ADECO_HD inline int piece_step(const float p[12], int done, int &face, int &mask, bool &last)
 {
-    const int b0 = face_bits(p[0], p[1], p[2]), b1 = face_bits(p[3], p[4], p[5]);
-    const int b2 = face_bits(p[6], p[7], p[8]), b3 = face_bits(p[9], p[10], p[11]);
-    const int all_in = b0 & b1 & b2 & b3, any_in = b0 | b1 | b2 | b3;
-    const int relevant = (63 >> face0) << face0;
-    if ((~any_in) & relevant) return 0;  // entirely outside a remaining face
-    const int next = (~all_in) & relevant;
-    if (!next) return 1;
-#ifdef __CUDA_ARCH__
-    face = __ffs(next) - 1;
-#else
-    face = __builtin_ctz(next);
-#endif
-    mask = ((b0 >> face) & 1) | (((b1 >> face) & 1) << 1) | (((b2 >> face) & 1) << 2) | (((b3 >> face) & 1) << 3);
-    if (last) *last = (next >> (face + 1)) == 0;
-    return 2;
+    return next_face(face_bits(p[0], p[1], p[2]), face_bits(p[3], p[4], p[5]), face_bits(p[6], p[7], p[8]),
+                     face_bits(p[9], p[10], p[11]), done, face, mask, last);
 }
 
-// Serial clipping of one piece from face `face0` on (used when the warp pool
-// is full): depth-first over the same splits and last-face fractions, so the
+// Serial clipping of one piece whose faces in `done0` are done (used when the
+// warp pool is full): depth-first over the same splits and last-face fractions, so the
 // fixed-point sum is the warp engine's.
 #ifdef __CUDA_ARCH__
 __device__ __noinline__
 #else
 inline
 #endif
-long long clip_piece_serial(const float p0[12], int face0)
+long long clip_piece_serial(const float p0[12], int done0)
 {
     constexpr int kDepth = 16;  // 2 pending pieces per face level + 3
     float stk[kDepth][12];
-    int sface[kDepth];
+    int sdone[kDepth];
 #pragma unroll
     for (int x = 0; x < 12; ++x) stk[0][x] = p0[x];
-    sface[0] = face0;
+    sdone[0] = done0;
     int sp = 1;
     long long acc = 0;
     while (sp > 0) {
@@ -423,7 +451,7 @@ long long clip_piece_serial(const float p0[12], int face0)
         for (int x = 0; x < 12; ++x) p[x] = stk[sp][x];
         int face = 0, mask = 0;
         bool last = false;
-        const int code = piece_step(p, sface[sp], face, mask, &last);
+        const int code = piece_step(p, sdone[sp], face, mask, last);
         if (code == 0) continue;
         if (code == 1 || last) {
             acc += vol_fixed(piece_vol6(p) * (code == 1 ? 1.f : inside_fraction(p, mask, face)));
@@ -432,18 +460,19 @@ long long clip_piece_serial(const float p0[12], int face0)
         float c0[12], c1[12], c2[12];
         const int n = split_piece(p, mask, face, c0, c1, c2);
         if (sp + 3 > kDepth) continue;  // cannot happen (depth <= 2*5 + 3)
+        const int d = sdone[sp] | (1 << face);
 #pragma unroll
         for (int x = 0; x < 12; ++x) stk[sp][x] = c0[x];
-        sface[sp] = face + 1;
+        sdone[sp] = d;
         ++sp;
         if (n == 3) {
 #pragma unroll
             for (int x = 0; x < 12; ++x) stk[sp][x] = c1[x];
-            sface[sp] = face + 1;
+            sdone[sp] = d;
             ++sp;
 #pragma unroll
             for (int x = 0; x < 12; ++x) stk[sp][x] = c2[x];
-            sface[sp] = face + 1;
+            sdone[sp] = d;
             ++sp;
         }
     }
@@ -464,7 +493,7 @@ constexpr int kPairs = 128;  // partial pairs per warp list
 
 struct WarpPool {
     float v[12][kPool];
-    uint32_t meta[kPool];     // owner | face << 8
+    uint32_t meta[kPool];     // owner | faces done << 8
     long long vacc[kPairs];   // 6x volume of each listed pair, fixed point 2^kVolShift
 };
 
@@ -483,7 +512,7 @@ __device__ __forceinline__ void clip_pairs(WarpPool &pool, int np, Build build, 
     __syncwarp();
     bool valid = false;
     float p[12];
-    int owner = 0, face = 0;
+    int owner = 0, done = 0;  // the piece's pair and its faces done (one bit per face)
     int top = 0, next = 0;
     for (;;) {
         // refill idle lanes
@@ -496,14 +525,14 @@ __device__ __forceinline__ void clip_pairs(WarpPool &pool, int np, Build build, 
                 for (int x = 0; x < 12; ++x) p[x] = pool.v[x][idx];
                 const uint32_t m = pool.meta[idx];
                 owner = (int)(m & 0xff);
-                face = (int)(m >> 8);
+                done = (int)(m >> 8);
                 valid = true;
             } else {
                 const int j = next + rank - top;
                 if (j < np) {
                     build(j, p);
                     owner = j;
-                    face = 0;
+                    done = 0;
                     valid = true;
                 }
             }
@@ -523,7 +552,7 @@ __device__ __forceinline__ void clip_pairs(WarpPool &pool, int np, Build build, 
         // had put most of the fine-grid time into one-lane serial clipping.
         int f = 0, mask = 0, code = 0;
         bool last = false;
-        if (valid) code = piece_step(p, face, f, mask, &last);
+        if (valid) code = piece_step(p, done, f, mask, last);
         const bool split = valid && code == 2 && !last;
         const int want = (split && split_kin(mask) != 1) ? 2 : 0;  // children to push
         int incl = want;
@@ -543,10 +572,10 @@ __device__ __forceinline__ void clip_pairs(WarpPool &pool, int np, Build build, 
                 split_piece(p, mask, f, c0, c1, c2);
 #pragma unroll
                 for (int x = 0; x < 12; ++x) p[x] = c0[x];
-                face = f + 1;
+                done |= 1 << f;
                 if (want) {
                     const int base = top + incl - want;
-                    const uint32_t m = (uint32_t)owner | ((uint32_t)face << 8);
+                    const uint32_t m = (uint32_t)owner | ((uint32_t)done << 8);
 #pragma unroll
                     for (int x = 0; x < 12; ++x) {
                         pool.v[x][base] = c1[x];
@@ -569,7 +598,7 @@ __device__ __forceinline__ void clip_pairs(WarpPool &pool, int np, Build build, 
             float q[12];
 #pragma unroll
             for (int x = 0; x < 12; ++x) q[x] = p[x];
-            const long long acc = clip_piece_serial(q, face);
+            const long long acc = clip_piece_serial(q, done);
             atomicAdd(reinterpret_cast<unsigned long long *>(&pool.vacc[owner]), (unsigned long long)acc);
             valid = false;
             ++fallbacks;
@@ -592,7 +621,7 @@ constexpr int kBaryList = 64;  // partial cells per warp list
 
 struct BaryPool {
     float v[kBaryRec][kBaryPool];
-    uint32_t meta[kBaryPool];  // owner | face << 8
+    uint32_t meta[kBaryPool];  // owner | faces done << 8
     long long acc[kBaryList];  // share of each listed cell, fixed point 2^kVolShift
     uint32_t cell[kBaryList];  // the listed cells (the caller's encoding)
 };
@@ -603,22 +632,11 @@ __device__ __forceinline__ float bary_val(const float *r, int v, int i)
     return i < 4 ? r[4 * v + i] : r[16 + 3 * v + (i - 4)];
 }
 
-// next face of a piece whose faces below face0 are done: 0 beyond a face
-// (dropped), 1 inside the rest (finished), 2 crossing `face` (mask: its
-// vertices inside; last: no later face is crossed)
-__device__ __forceinline__ int bary_step(const float *r, int face0, int &face, int &mask, bool &last)
+// next_face of a barycentric piece whose faces in `done` are done
+__device__ __forceinline__ int bary_step(const float *r, int done, int &face, int &mask, bool &last)
 {
-    const int b0 = face_bits(r[16], r[17], r[18]), b1 = face_bits(r[19], r[20], r[21]);
-    const int b2 = face_bits(r[22], r[23], r[24]), b3 = face_bits(r[25], r[26], r[27]);
-    const int all_in = b0 & b1 & b2 & b3, any_in = b0 | b1 | b2 | b3;
-    const int relevant = (63 >> face0) << face0;
-    if ((~any_in) & relevant) return 0;
-    const int next = (~all_in) & relevant;
-    if (!next) return 1;
-    face = __ffs(next) - 1;
-    mask = ((b0 >> face) & 1) | (((b1 >> face) & 1) << 1) | (((b2 >> face) & 1) << 2) | (((b3 >> face) & 1) << 3);
-    last = (next >> (face + 1)) == 0;
-    return 2;
+    return next_face(face_bits(r[16], r[17], r[18]), face_bits(r[19], r[20], r[21]), face_bits(r[22], r[23], r[24]),
+                     face_bits(r[25], r[26], r[27]), done, face, mask, last);
 }
 
 __device__ __forceinline__ float bary_last_fraction(const float *r, int f, int mask)
@@ -703,7 +721,7 @@ __device__ __forceinline__ void clip_bary_pairs(BaryPool &pool, int np, Build bu
     __syncwarp();
     bool valid = false;
     float r[kBaryRec];
-    int owner = 0, face = 0;
+    int owner = 0, done = 0;  // the piece's cell and its faces done (one bit per face)
     int top = 0, next = 0;
     for (;;) {
         // refill idle lanes: pool first (last in, first out), then the list
@@ -716,14 +734,14 @@ __device__ __forceinline__ void clip_bary_pairs(BaryPool &pool, int np, Build bu
                 for (int x = 0; x < kBaryRec; ++x) r[x] = pool.v[x][idx];
                 const uint32_t m = pool.meta[idx];
                 owner = (int)(m & 0xff);
-                face = (int)(m >> 8);
+                done = (int)(m >> 8);
                 valid = true;
             } else {
                 const int j = next + rank - top;
                 if (j < np) {
                     build(j, r);
                     owner = j;
-                    face = 0;
+                    done = 0;
                     valid = true;
                 }
             }
@@ -739,7 +757,7 @@ __device__ __forceinline__ void clip_bary_pairs(BaryPool &pool, int np, Build bu
         // move
         int f = 0, mask = 0, code = 0;
         bool last = false;
-        if (valid) code = bary_step(r, face, f, mask, last);
+        if (valid) code = bary_step(r, done, f, mask, last);
         const bool want_split = valid && code == 2 && !last;
         const int want = (want_split && split_kin(mask) != 1) ? 2 : 0;
         int incl = want;
@@ -760,10 +778,10 @@ __device__ __forceinline__ void clip_bary_pairs(BaryPool &pool, int np, Build bu
             if (want_split) {
                 bary_split(r, f, mask, P, E, k);
                 split = true;
-                face = f + 1;
+                done |= 1 << f;
                 if (want) {
                     const int base = top + incl - want;
-                    const uint32_t m = (uint32_t)owner | ((uint32_t)face << 8);
+                    const uint32_t m = (uint32_t)owner | ((uint32_t)done << 8);
 #pragma unroll
                     for (int x = 0; x < kBaryRec; ++x) {
                         pool.v[x][base] = bary_child(P, E, k, 1, x);
@@ -784,7 +802,7 @@ __device__ __forceinline__ void clip_bary_pairs(BaryPool &pool, int np, Build bu
 #pragma unroll
             for (int x = 0; x < kBaryRec; ++x) q[x] = r[x];
             atomicAdd(reinterpret_cast<unsigned long long *>(&pool.acc[owner]),
-                      (unsigned long long)share_fixed(clip_bary_serial(q, face)));
+                      (unsigned long long)share_fixed(clip_bary_serial(q, done)));
             valid = false;
             ++fallbacks;
         }
