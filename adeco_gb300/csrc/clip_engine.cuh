@@ -480,14 +480,6 @@ long long clip_piece_serial(const float p0[12], int done0)
 }
 
 #ifdef __CUDACC__
-// warp-wide maximum of a non-negative int (butterfly of shuffles)
-__device__ __forceinline__ int warp_max(int v)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
-    return v;
-}
-
 constexpr int kPool = 56;    // pieces per warp pool (2 CTAs of 8 warps fit in an SM's shared memory)
 constexpr int kPairs = 128;  // partial pairs per warp list
 
@@ -540,31 +532,28 @@ __device__ __forceinline__ void clip_pairs(WarpPool &pool, int np, Build build, 
         const int from_pool = nneed < top ? nneed : top;
         top -= from_pool;
         next = min(np, next + (nneed - from_pool));
-        if (!__any_sync(0xffffffffu, valid)) break;
-        __syncwarp();
-        // one step.  A lane about to split reserves room in the pool for its
-        // extra children first (a warp-wide scan); a lane whose children do
-        // not fit keeps its piece and steps again next round, while the other
-        // lanes finish pieces and idle lanes drain the pool.  The lanes that
-        // fit are a prefix of the scan.  Only when every lane holds a piece
-        // and none can move does one lane clip its piece alone (serially, with
-        // a local stack): letting every pushing lane of a full pool do that
-        // had put most of the fine-grid time into one-lane serial clipping.
+        const unsigned held = __ballot_sync(0xffffffffu, valid);
+        if (!held) break;
+        __syncwarp();  // the pool slots just read may be written by this step's pushes
+        // one step.  A lane about to split into three reserves room in the
+        // pool for its two extra children first: in lane order, as many as
+        // fit.  A lane whose children do not fit keeps its piece and steps
+        // again next round, while the other lanes finish pieces and idle lanes
+        // drain the pool.  Only when every lane holds a piece and none can
+        // move does one lane clip its piece alone (serially, with a local
+        // stack): letting every pushing lane of a full pool do that had put
+        // most of the fine-grid time into one-lane serial clipping.
         int f = 0, mask = 0, code = 0;
         bool last = false;
         if (valid) code = piece_step(p, done, f, mask, last);
         const bool split = valid && code == 2 && !last;
-        const int want = (split && split_kin(mask) != 1) ? 2 : 0;  // children to push
-        int incl = want;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += y;
-        }
-        const bool defer = want && (top + incl > kPool);
-        const unsigned moving = __ballot_sync(0xffffffffu, valid && !defer);
-        const unsigned deferred = __ballot_sync(0xffffffffu, defer);
-        const bool stuck = moving == 0u && __ballot_sync(0xffffffffu, valid) == 0xffffffffu;
+        const bool push = split && split_kin(mask) != 1;  // two children to push
+        const unsigned pushing = __ballot_sync(0xffffffffu, push);
+        const int fit = (kPool - top) >> 1;  // pushing lanes whose children fit
+        const int prank = __popc(pushing & lt);
+        const bool defer = push && prank >= fit;
+        const int nfit = min(__popc(pushing), fit);
+        const bool stuck = held == 0xffffffffu && pushing == 0xffffffffu && fit == 0;
         if (valid && !defer) {
             long long v = 0;
             if (split) {
@@ -573,8 +562,8 @@ __device__ __forceinline__ void clip_pairs(WarpPool &pool, int np, Build build, 
 #pragma unroll
                 for (int x = 0; x < 12; ++x) p[x] = c0[x];
                 done |= 1 << f;
-                if (want) {
-                    const int base = top + incl - want;
+                if (push) {
+                    const int base = top + 2 * prank;
                     const uint32_t m = (uint32_t)owner | ((uint32_t)done << 8);
 #pragma unroll
                     for (int x = 0; x < 12; ++x) {
@@ -591,7 +580,7 @@ __device__ __forceinline__ void clip_pairs(WarpPool &pool, int np, Build build, 
                 valid = false;
             }
             if (v) atomicAdd(reinterpret_cast<unsigned long long *>(&pool.vacc[owner]), (unsigned long long)v);
-        } else if (stuck && lane == __ffs(deferred) - 1) {
+        } else if (stuck && lane == 0) {
             // a copy made here: handing p itself to the out-of-line routine
             // takes its address, and p then lives in local memory, stored
             // there on every step although this branch almost never runs
@@ -603,7 +592,7 @@ __device__ __forceinline__ void clip_pairs(WarpPool &pool, int np, Build build, 
             valid = false;
             ++fallbacks;
         }
-        top += warp_max((want && !defer) ? incl : 0);
+        top += 2 * nfit;
         __syncwarp();
     }
     __syncwarp();
@@ -749,8 +738,9 @@ __device__ __forceinline__ void clip_bary_pairs(BaryPool &pool, int np, Build bu
         const int from_pool = nneed < top ? nneed : top;
         top -= from_pool;
         next = min(np, next + (nneed - from_pool));
-        if (!__any_sync(0xffffffffu, valid)) break;
-        __syncwarp();
+        const unsigned held = __ballot_sync(0xffffffffu, valid);
+        if (!held) break;
+        __syncwarp();  // the pool slots just read may be written by this step's pushes
         // one step, with the main engine's pool reservation: a lane whose two
         // extra children do not fit keeps its piece for the next round; one
         // lane clips serially only when every lane holds a piece and none can
@@ -759,17 +749,13 @@ __device__ __forceinline__ void clip_bary_pairs(BaryPool &pool, int np, Build bu
         bool last = false;
         if (valid) code = bary_step(r, done, f, mask, last);
         const bool want_split = valid && code == 2 && !last;
-        const int want = (want_split && split_kin(mask) != 1) ? 2 : 0;
-        int incl = want;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += y;
-        }
-        const bool defer = want && (top + incl > kBaryPool);
-        const unsigned moving = __ballot_sync(0xffffffffu, valid && !defer);
-        const unsigned deferred = __ballot_sync(0xffffffffu, defer);
-        const bool stuck = moving == 0u && __ballot_sync(0xffffffffu, valid) == 0xffffffffu;
+        const bool push = want_split && split_kin(mask) != 1;
+        const unsigned pushing = __ballot_sync(0xffffffffu, push);
+        const int fit = (kBaryPool - top) >> 1;
+        const int prank = __popc(pushing & lt);
+        const bool defer = push && prank >= fit;
+        const int nfit = min(__popc(pushing), fit);
+        const bool stuck = held == 0xffffffffu && pushing == 0xffffffffu && fit == 0;
         int k = 1;
         bool split = false;
         float P[4][7], E[4][7];
@@ -779,8 +765,8 @@ __device__ __forceinline__ void clip_bary_pairs(BaryPool &pool, int np, Build bu
                 bary_split(r, f, mask, P, E, k);
                 split = true;
                 done |= 1 << f;
-                if (want) {
-                    const int base = top + incl - want;
+                if (push) {
+                    const int base = top + 2 * prank;
                     const uint32_t m = (uint32_t)owner | ((uint32_t)done << 8);
 #pragma unroll
                     for (int x = 0; x < kBaryRec; ++x) {
@@ -797,7 +783,7 @@ __device__ __forceinline__ void clip_bary_pairs(BaryPool &pool, int np, Build bu
             }
             const long long v = share_fixed(c);
             if (v) atomicAdd(reinterpret_cast<unsigned long long *>(&pool.acc[owner]), (unsigned long long)v);
-        } else if (stuck && lane == __ffs(deferred) - 1) {
+        } else if (stuck && lane == 0) {
             float q[kBaryRec];  // a copy, so that r itself never needs an address (see clip_pairs)
 #pragma unroll
             for (int x = 0; x < kBaryRec; ++x) q[x] = r[x];
@@ -806,7 +792,7 @@ __device__ __forceinline__ void clip_bary_pairs(BaryPool &pool, int np, Build bu
             valid = false;
             ++fallbacks;
         }
-        top += warp_max((want && !defer) ? incl : 0);
+        top += 2 * nfit;
         if (split) {
 #pragma unroll
             for (int x = 0; x < kBaryRec; ++x) r[x] = bary_child(P, E, k, 0, x);
