@@ -84,87 +84,103 @@ ADECO_HD inline float rcp_nr(float d)
 #endif
 }
 
-// point where edge in->out crosses the plane x_axis = plane (snapped onto it)
-ADECO_HD inline void cut_point(const float *pin, const float *pout, int axis, float plane, float *x)
-{
-    const float din = sel3(axis, pin[0], pin[1], pin[2]);
-    const float dout = sel3(axis, pout[0], pout[1], pout[2]);
-    float t = (plane - din) * rcp_nr(dout - din);  // |dout - din| > 0 for a crossing edge
-    t = fminf(fmaxf(t, 0.f), 1.f);
-    x[0] = (axis == 0) ? plane : fmaf(t, pout[0] - pin[0], pin[0]);
-    x[1] = (axis == 1) ? plane : fmaf(t, pout[1] - pin[1], pin[1]);
-    x[2] = (axis == 2) ? plane : fmaf(t, pout[2] - pin[2], pin[2]);
-}
+// The cut of piece p by face f (mask: its vertices inside, 0 < mask < 15;
+// k of them), shared by a split and a last-face fraction: the vertices
+// permuted to A B C D, inside first by an even permutation (the orientation
+// is kept), the four cut edges' end points -- k=1: AB AC AD AD; k=2: AC AD
+// BC BD; k=3: AD BD CD CD -- and on each edge the reciprocal r of its extent
+// along the face's axis and the face's parameter t from the inside end.
+struct Cut {
+    float A[3], B[3], C[3], D[3];
+    float i[4][3], o[4][3];
+    float t[4], r[4];
+    int k;
+};
 
-// Inside part of piece p w.r.t. face f (mask = 4-bit inside flags, 0 < mask <
-// 15) as n = 1 or 3 positively oriented pieces c0..c2.  With the vertices
-// permuted to A B C D (inside first, even permutation) and k inside:
-//   k = 1: (A, Xab, Xac, Xad)
-//   k = 2: (A, B, Xbc, Xbd) (A, Xbc, Xac, Xbd) (A, Xac, Xad, Xbd)
-//   k = 3: (A, B, C, Xcd)  (A, B, Xcd, Xbd) (A, Xbd, Xcd, Xad)
-// written as one code path: four cut points E0..E3 chosen by k, then the
-// children's vertices picked by k.
-ADECO_HD inline void put(float *dst, const float *a, const float *b, const float *c, const float *d)
-{
-#pragma unroll
-    for (int x = 0; x < 3; ++x) {
-        dst[x] = a[x];
-        dst[3 + x] = b[x];
-        dst[6 + x] = c[x];
-        dst[9 + x] = d[x];
-    }
-}
-
-ADECO_HD inline int split_piece(const float p[12], int mask, int f, float c0[12], float c1[12], float c2[12])
+ADECO_HD inline void cut_piece(const float p[12], int mask, int f, Cut &c)
 {
     const int axis = f >> 1;
     const float plane = (f & 1) ? 1.f : 0.f;
     const int pm = split_perm(mask), k = split_kin(mask);
+    c.k = k;
     const int ia = pm & 3, ib = (pm >> 2) & 3, ic = (pm >> 4) & 3, id = (pm >> 6) & 3;
-    float A[3], B[3], C[3], D[3];
 #pragma unroll
     for (int x = 0; x < 3; ++x) {
-        A[x] = sel4(ia, p[x], p[3 + x], p[6 + x], p[9 + x]);
-        B[x] = sel4(ib, p[x], p[3 + x], p[6 + x], p[9 + x]);
-        C[x] = sel4(ic, p[x], p[3 + x], p[6 + x], p[9 + x]);
-        D[x] = sel4(id, p[x], p[3 + x], p[6 + x], p[9 + x]);
+        c.A[x] = sel4(ia, p[x], p[3 + x], p[6 + x], p[9 + x]);
+        c.B[x] = sel4(ib, p[x], p[3 + x], p[6 + x], p[9 + x]);
+        c.C[x] = sel4(ic, p[x], p[3 + x], p[6 + x], p[9 + x]);
+        c.D[x] = sel4(id, p[x], p[3 + x], p[6 + x], p[9 + x]);
+        c.i[0][x] = c.A[x];
+        c.o[0][x] = (k == 1) ? c.B[x] : ((k == 2) ? c.C[x] : c.D[x]);
+        c.i[1][x] = (k == 3) ? c.B[x] : c.A[x];
+        c.o[1][x] = (k == 1) ? c.C[x] : c.D[x];
+        c.i[2][x] = (k == 1) ? c.A[x] : ((k == 2) ? c.B[x] : c.C[x]);
+        c.o[2][x] = (k == 2) ? c.C[x] : c.D[x];
+        c.i[3][x] = (k == 2) ? c.B[x] : ((k == 3) ? c.C[x] : c.A[x]);
+        c.o[3][x] = c.D[x];
     }
-    // edge end points: k=1: AB AC AD AD; k=2: AC AD BC BD; k=3: AD BD CD CD
-    float i0[3], o0[3], i1[3], o1[3], i2[3], o2[3], i3[3], o3[3];
 #pragma unroll
-    for (int x = 0; x < 3; ++x) {
-        i0[x] = A[x];
-        o0[x] = (k == 1) ? B[x] : ((k == 2) ? C[x] : D[x]);
-        i1[x] = (k == 3) ? B[x] : A[x];
-        o1[x] = (k == 1) ? C[x] : D[x];
-        i2[x] = (k == 1) ? A[x] : ((k == 2) ? B[x] : C[x]);
-        o2[x] = (k == 2) ? C[x] : D[x];
-        i3[x] = (k == 2) ? B[x] : ((k == 3) ? C[x] : A[x]);
-        o3[x] = D[x];
+    for (int e = 0; e < 4; ++e) {
+        const float din = sel3(axis, c.i[e][0], c.i[e][1], c.i[e][2]);
+        const float dout = sel3(axis, c.o[e][0], c.o[e][1], c.o[e][2]);
+        c.r[e] = rcp_nr(dout - din);  // |dout - din| > 0 on a crossing edge
+        c.t[e] = fminf(fmaxf((plane - din) * c.r[e], 0.f), 1.f);
     }
-    float E0[3], E1[3], E2[3], E3[3];
-    cut_point(i0, o0, axis, plane, E0);
-    cut_point(i1, o1, axis, plane, E1);
-    cut_point(i2, o2, axis, plane, E2);
-    cut_point(i3, o3, axis, plane, E3);
+}
+
+// Inside part of a cut piece as n = 1 or 3 positively oriented pieces
+// c0..c2, from the cut points E0..E3 of the cut's edges (snapped onto the
+// face):
+//   k = 1: (A, Xab, Xac, Xad)
+//   k = 2: (A, B, Xbc, Xbd) (A, Xbc, Xac, Xbd) (A, Xac, Xad, Xbd)
+//   k = 3: (A, B, C, Xcd)  (A, B, Xcd, Xbd) (A, Xbd, Xcd, Xad)
+// written as one code path: the children's vertices picked by k.
+ADECO_HD inline int split_cut(const Cut &c, int f, float c0[12], float c1[12], float c2[12])
+{
+    const int axis = f >> 1;
+    const float plane = (f & 1) ? 1.f : 0.f;
+    float E[4][3];
+#pragma unroll
+    for (int e = 0; e < 4; ++e)
+#pragma unroll
+        for (int x = 0; x < 3; ++x)
+            E[e][x] = (x == axis) ? plane : fmaf(c.t[e], c.o[e][x] - c.i[e][x], c.i[e][x]);
     // k=1: E0=Xab E1=Xac E2=Xad | k=2: E0=Xac E1=Xad E2=Xbc E3=Xbd | k=3: E0=Xad E1=Xbd E2=Xcd
-    const bool k1 = (k == 1), k2 = (k == 2);
+    const bool k1 = (c.k == 1), k2 = (c.k == 2);
 #pragma unroll
     for (int x = 0; x < 3; ++x) {
-        c0[x] = A[x];
-        c0[3 + x] = k1 ? E0[x] : B[x];
-        c0[6 + x] = k1 ? E1[x] : (k2 ? E2[x] : C[x]);
-        c0[9 + x] = k1 ? E2[x] : (k2 ? E3[x] : E2[x]);
-        c1[x] = A[x];
-        c1[3 + x] = k2 ? E2[x] : B[x];
-        c1[6 + x] = k2 ? E0[x] : E2[x];
-        c1[9 + x] = k2 ? E3[x] : E1[x];
-        c2[x] = A[x];
-        c2[3 + x] = k2 ? E0[x] : E1[x];
-        c2[6 + x] = k2 ? E1[x] : E2[x];
-        c2[9 + x] = k2 ? E3[x] : E0[x];
+        c0[x] = c.A[x];
+        c0[3 + x] = k1 ? E[0][x] : c.B[x];
+        c0[6 + x] = k1 ? E[1][x] : (k2 ? E[2][x] : c.C[x]);
+        c0[9 + x] = k1 ? E[2][x] : (k2 ? E[3][x] : E[2][x]);
+        c1[x] = c.A[x];
+        c1[3 + x] = k2 ? E[2][x] : c.B[x];
+        c1[6 + x] = k2 ? E[0][x] : E[2][x];
+        c1[9 + x] = k2 ? E[3][x] : E[1][x];
+        c2[x] = c.A[x];
+        c2[3 + x] = k2 ? E[0][x] : E[1][x];
+        c2[6 + x] = k2 ? E[1][x] : E[2][x];
+        c2[9 + x] = k2 ? E[3][x] : E[0][x];
     }
     return k1 ? 1 : 3;
+}
+
+// The fraction of a cut piece inside the face (its last crossed face), from
+// the edge parameters alone: t from the cut, u = 1 - t taken as (x_o -
+// plane) r so both keep their relative precision (side_fraction's formulas,
+// on the same edges).
+ADECO_HD inline float cut_fraction(const Cut &c, int f)
+{
+    const int axis = f >> 1;
+    const float plane = (f & 1) ? 1.f : 0.f;
+    float u[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e)
+        u[e] = fminf(fmaxf((sel3(axis, c.o[e][0], c.o[e][1], c.o[e][2]) - plane) * c.r[e], 0.f), 1.f);
+    const float *t = c.t;
+    if (c.k == 1) return t[0] * t[1] * t[2];
+    if (c.k == 2) return fmaf(t[2], t[3], t[0] * (t[3] * u[2] + t[1] * u[3]));
+    return fmaf(u[0], fmaf(u[1], t[2], t[1]), t[0]);
 }
 
 // Fraction of piece p inside face f (mask = 4-bit inside flags, 0 < mask <
@@ -184,7 +200,7 @@ ADECO_HD inline float side_fraction(float x0, float x1, float x2, float x3, int 
     const int pm = split_perm(mask), k = split_kin(mask);
     const float a = sel4(pm & 3, x0, x1, x2, x3), b = sel4((pm >> 2) & 3, x0, x1, x2, x3);
     const float c = sel4((pm >> 4) & 3, x0, x1, x2, x3), d = sel4((pm >> 6) & 3, x0, x1, x2, x3);
-    // edges as in split_piece: k=1: AB AC AD; k=2: AC AD BC BD; k=3: AD BD CD
+    // edges as in cut_piece: k=1: AB AC AD; k=2: AC AD BC BD; k=3: AD BD CD
     const float i0 = a, o0 = (k == 1) ? b : ((k == 2) ? c : d);
     const float i1 = (k == 3) ? b : a, o1 = (k == 1) ? c : d;
     const float i2 = (k == 1) ? a : ((k == 2) ? b : c), o2 = (k == 2) ? c : d;
@@ -202,14 +218,6 @@ ADECO_HD inline float side_fraction(float x0, float x1, float x2, float x3, int 
     if (k == 1) return t[0] * t[1] * t[2];
     if (k == 2) return fmaf(t[2], t[3], t[0] * (t[3] * u[2] + t[1] * u[3]));
     return fmaf(u[0], fmaf(u[1], t[2], t[1]), t[0]);
-}
-
-ADECO_HD inline float inside_fraction(const float p[12], int mask, int f)
-{
-    const int axis = f >> 1;
-    const float x0 = sel3(axis, p[0], p[1], p[2]), x1 = sel3(axis, p[3], p[4], p[5]);
-    const float x2 = sel3(axis, p[6], p[7], p[8]), x3 = sel3(axis, p[9], p[10], p[11]);
-    return side_fraction(x0, x1, x2, x3, mask, (f & 1) ? 1.f : 0.f);
 }
 
 // Values of a linear function G(u) = G0 + n.u at the unit cube's 8 corners
@@ -366,7 +374,7 @@ F2 clip_bary_serial(const float *rec0, int done0)
             acc = f2_add(acc, f2_mul_f(bary_share(w), side_fraction(xa[0], xa[1], xa[2], xa[3], mask, plane)));
             continue;
         }
-        // split by face f into 1 or 3 pieces (vertex patterns of split_piece)
+        // split by face f into 1 or 3 pieces (vertex patterns of split_cut)
         const int pm = split_perm(mask), k = split_kin(mask);
         const int id[4] = {pm & 3, (pm >> 2) & 3, (pm >> 4) & 3, (pm >> 6) & 3};
         // edges: k=1: AB AC AD; k=2: AC AD BC BD; k=3: AD BD CD
@@ -453,12 +461,18 @@ long long clip_piece_serial(const float p0[12], int done0)
         bool last = false;
         const int code = piece_step(p, sdone[sp], face, mask, last);
         if (code == 0) continue;
-        if (code == 1 || last) {
-            acc += vol_fixed(piece_vol6(p) * (code == 1 ? 1.f : inside_fraction(p, mask, face)));
+        if (code == 1) {
+            acc += vol_fixed(piece_vol6(p));
+            continue;
+        }
+        Cut cut;
+        cut_piece(p, mask, face, cut);
+        if (last) {
+            acc += vol_fixed(piece_vol6(p) * cut_fraction(cut, face));
             continue;
         }
         float c0[12], c1[12], c2[12];
-        const int n = split_piece(p, mask, face, c0, c1, c2);
+        const int n = split_cut(cut, face, c0, c1, c2);
         if (sp + 3 > kDepth) continue;  // cannot happen (depth <= 2*5 + 3)
         const int d = sdone[sp] | (1 << face);
 #pragma unroll
@@ -556,9 +570,14 @@ __device__ __forceinline__ void clip_pairs(WarpPool &pool, int np, Build build, 
         const bool stuck = held == 0xffffffffu && pushing == 0xffffffffu && fit == 0;
         if (valid && !defer) {
             long long v = 0;
+            // the cut is shared by the lanes that split and the lanes at
+            // their last crossed face, so the warp runs it once per step
+            float frac = 1.f;
+            Cut cut;
+            if (code == 2) cut_piece(p, mask, f, cut);
             if (split) {
                 float c0[12], c1[12], c2[12];
-                split_piece(p, mask, f, c0, c1, c2);
+                split_cut(cut, f, c0, c1, c2);
 #pragma unroll
                 for (int x = 0; x < 12; ++x) p[x] = c0[x];
                 done |= 1 << f;
@@ -576,7 +595,8 @@ __device__ __forceinline__ void clip_pairs(WarpPool &pool, int np, Build build, 
             } else {
                 // finished, or at its last crossed face: the inside part
                 // needs no more clipping, so its volume is added here
-                if (code != 0) v = vol_fixed(piece_vol6(p) * (code == 1 ? 1.f : inside_fraction(p, mask, f)));
+                if (code == 2) frac = cut_fraction(cut, f);
+                if (code != 0) v = vol_fixed(piece_vol6(p) * frac);
                 valid = false;
             }
             if (v) atomicAdd(reinterpret_cast<unsigned long long *>(&pool.vacc[owner]), (unsigned long long)v);
