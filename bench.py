@@ -212,14 +212,15 @@ def set_workload(name):
     """c2: the benchmark (256^3 octree deposit).  c4: 512^3 lattice with 2000
     infall regions (seed 4), octree depth <= 12.  c1: 64^3 periodic lattice
     onto a uniform 128^3 grid through the reference boundary.  zoom and serve
-    run on the c2 lattice."""
+    run on the c2 lattice; c5 serves zoom requests of 32^3 to 512^3 cells
+    against the resident c4 lattice."""
     global N_PART, SEED, INFALL, MAX_LEVEL, WORKLOAD, RMS_DISP
     if name == "c1":
         N_PART, SEED, RMS_DISP = 64, 0, 0.5
         WORKLOAD = ("periodic 64^3 Zel'dovich lattice (rms disp 0.5 spacings, seed 0, L=100; 64^3 cubes = 1,572,864 "
                     "tets from ghost planes shifted by +L, 64 patches of 16^3 cubes) onto a uniform 128^3 grid over "
                     "the box through the reference boundary; periodic wrap = sum over the box's 27 images")
-    if name == "c4":
+    if name in ("c4", "c5"):
         N_PART, SEED, INFALL, MAX_LEVEL = 512, 4, 2000, 12
         WORKLOAD = ("octree deposit of a 512^3 Zel'dovich lattice with 2000 infall regions (rms disp 3 spacings, "
                     "seed 4, L=100): depth <= 12, 16^3-cell leaves, refine while tet estimate > 262144")
@@ -806,7 +807,9 @@ def run_serve(args, rank, ws, local):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"Poisson arrivals at {args.serve_rate:g} req/s for {args.serve_seconds:g} s "
                                f"(seed {SERVE_SEED}): zoom boxes, side log-uniform [0.005L, 0.5L], resolution from "
-                               f"{args.serve_dims}, on the 256^3 lattice (seed 0); one batch per request"},
+                               f"{args.serve_dims}, depth 0 (a uniform grid per request), on the resident "
+                               f"{N_PART}^3 lattice (seed {SEED}{', 2000 infall regions' if INFALL else ''}); "
+                               f"one batch per request"},
         "p50_ms": float(np.percentile(lat, 50)), "p90_ms": float(np.percentile(lat, 90)),
         "p99_ms": float(np.percentile(lat, 99)), "max_ms": float(lat[-1]),
         "requests": len(lat), "offered_rate": args.serve_rate, "achieved_rate": len(lat) / wall,
@@ -865,13 +868,13 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--n", type=int, default=None, help="lattice size; the benchmark workload is 256")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c4", "zoom", "serve"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c4", "zoom", "serve", "c5"])
     ap.add_argument("--zoom-dims", type=int, nargs="+", default=[32, 64, 128, 256])
     ap.add_argument("--zoom-count", type=int, default=ZOOM_COUNT)
-    ap.add_argument("--serve-rate", type=float, default=30.0)
-    ap.add_argument("--serve-rate-high", type=float, default=50.0, help="default run: a second serving load point (0: none)")
+    ap.add_argument("--serve-rate", type=float, default=None, help="req/s (30; c5: 10)")
+    ap.add_argument("--serve-rate-high", type=float, default=100.0, help="default run: a second serving load point (0: none)")
     ap.add_argument("--serve-seconds", type=float, default=8.0)
-    ap.add_argument("--serve-dims", type=int, nargs="+", default=[128])
+    ap.add_argument("--serve-dims", type=int, nargs="+", default=None, help="resolutions (128; c5: 32 .. 512)")
     ap.add_argument("--serve-drain-s", type=float, default=30.0)
     ap.add_argument("--skip-serve", action="store_true", help="default run: no serving leg")
     ap.add_argument("--skip-zoom", action="store_true", help="default run: no zoom-batch leg")
@@ -881,6 +884,11 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="library defaults instead of the autotuner")
     ap.add_argument("--retune", action="store_true", help="search again even when the tuning cache has a result")
     args = ap.parse_args()
+    c5 = args.workload == "c5"
+    if args.serve_rate is None:
+        args.serve_rate = 10.0 if c5 else 30.0
+    if args.serve_dims is None:
+        args.serve_dims = [32, 64, 128, 256, 512] if c5 else [128]
     set_workload(args.workload)
     if args.n:
         set_size(args.n)
@@ -891,7 +899,7 @@ def main():
         return run_reference(args, rank, ws)
     if args.workload == "zoom":
         return run_zoom(args, rank, ws, local)
-    if args.workload == "serve":
+    if args.workload in ("serve", "c5"):
         return run_serve(args, rank, ws, local)
     if args.workload == "c1":
         return run_c1(args, rank, ws, local)
