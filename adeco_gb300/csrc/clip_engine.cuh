@@ -63,27 +63,6 @@ ADECO_HD inline int face_bits(float x, float y, float z)
            ((int)(z > 0.f) << 4) | ((int)(z < 1.f) << 5);
 }
 
-// 1/d with round-to-nearest errors only: the hardware's approximate
-// reciprocal (PTX rcp.approx) refined by one Newton-Raphson step, r + r (1 -
-// d r) in fused multiply-adds.  Measured on GB300 over d log-uniform in
-// [2^-8, 2^4]: the approximate reciprocal's mean signed relative error is
-// +3.7e-9 (it errs the same way for most d), the refined one's 3.4e-12, the
-// same as the correctly rounded reciprocal's.  Through the edge parameters of
-// every cut point and last-face fraction the approximate one showed as a
-// total-mass excess of 4e-9 relative on a 96^3 lattice.  For the engine's
-// denominators: differences of cell-frame coordinates across a face, nonzero
-// and far from the float range limits.
-ADECO_HD inline float rcp_nr(float d)
-{
-#ifdef __CUDA_ARCH__
-    float r;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(d));
-    return fmaf(r, fmaf(-d, r, 1.f), r);
-#else
-    return 1.f / d;
-#endif
-}
-
 // The cut of piece p by face f (mask: its vertices inside, 0 < mask < 15;
 // k of them), shared by a split and a last-face fraction: the vertices
 // permuted to A B C D, inside first by an even permutation (the orientation

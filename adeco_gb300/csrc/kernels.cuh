@@ -328,8 +328,11 @@ ADECO_HD inline int setup_tet(const float3 vin[4], const float ghin[4][3], const
                                   F2{qf[fc[f]][a], ql[fc[f]][a]});
             dd = f2_add(dd, f2_mul_f(sum, nn[a]));
         }
-        const float d_hi = div_rn(dd.hi, 3.f);
-        const float d_lo = div_rn(fmaf(-d_hi, 3.f, dd.hi) + dd.lo, 3.f);
+        // / 3 as a product with 1/3: the remainder of d_hi is exact (fma) and
+        // carried into d_lo, so d_hi + d_lo keeps ~44 bits without a division
+        constexpr float kThird = 1.f / 3.f;
+        const float d_hi = dd.hi * kThird;
+        const float d_lo = (fmaf(-d_hi, 3.f, dd.hi) + dd.lo) * kThird;
         W.n[f][0][lane] = nx;
         W.n[f][1][lane] = ny;
         W.n[f][2][lane] = nz;
@@ -365,8 +368,9 @@ ADECO_HD inline int setup_tet(const float3 vin[4], const float ghin[4][3], const
             const float dx = qf[a0][0] - qf[b0][0], dy = qf[a0][1] - qf[b0][1], dz = qf[a0][2] - qf[b0][2];
             L2 = fmaxf(L2, dx * dx + dy * dy + dz * dz);
         }
-    const float Lm = sqrtf(L2);
-    *fp64_route = !(Lm * Lm * Lm <= kKappaFp64 * vq6);
+    // L^3 <= kappa |6V| squared (both sides non-negative): no square root;
+    // NaN or an overflow routes the tet
+    *fp64_route = !(L2 * L2 * L2 <= (kKappaFp64 * kKappaFp64) * (vq6 * vq6));
     return (hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
 }
 
