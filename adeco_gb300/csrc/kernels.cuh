@@ -663,7 +663,7 @@ ADECO_HD inline void piece_coords(const WarpTets &W, const GridDesc &g, int s, i
         nflip += flip;
 #pragma unroll
         for (int v = 0; v < 4; ++v)
-            p[3 * v + x] = cell_coord_sel(W.q[3 * v + x][s], W.qlo[3 * v + x][s], cc[x], g.drcell[x], flip);
+            p[3 * v + x] = cell_coord_fast(W.q[3 * v + x][s], W.qlo[3 * v + x][s], cc[x], g.drcell[x], flip);
     }
     if (nflip & 1) {
 #pragma unroll
