@@ -199,41 +199,64 @@ ADECO_HD inline float side_fraction(float x0, float x1, float x2, float x3, int 
     return fmaf(u[0], fmaf(u[1], t[2], t[1]), t[0]);
 }
 
-// Values of a linear function G(u) = G0 + n.u at the unit cube's 8 corners
-// (k: bit 0 x, bit 1 y, bit 2 z) from G0 as a double-float pair: each corner
-// value is formed exactly (TwoSum) and rounded once, so that a value near
-// zero -- a plane passing close to a corner, a thin sliver of the cube --
-// keeps its relative precision instead of the ~6e-8 |n| of an FP32 sum.
-ADECO_HD inline void cube_corner_values(F2 G0, float nx, float ny, float nz, float P[8])
+// 6x volume of the unit cube's part where G(u) = G0 + n.u > 0 (G0 a
+// double-float pair).  The cube is first reflected along every axis where
+// n_i < 0 (the volume does not change), so that n >= 0 and G grows along
+// every edge path from corner 0 to corner 7.  The corner values are then
+// formed exactly (TwoSum) and rounded once, which keeps that order, and the
+// cube is split into the 6 tets around the diagonal 0-7, each of 6x volume 1:
+// tet (0, a, b, 7) for the paths a -> b in {1,2,4} -> {3,5,6}, with values
+// g0 <= ga <= gb <= g7.  The part of a tet where G > 0 is then a suffix of its
+// path, and its fraction comes from the parameters t = g_in / (g_in - g_out)
+// and u = 1 - t = -g_out / (g_in - g_out) of its crossing edges:
+//   only 7 inside (gb <= 0 < g7):  t_70 t_7a t_7b        (the corner tet)
+//   7, b inside (ga <= 0 < gb):    t_b0 t_ba + t_70 t_ba u_b0 + t_70 t_7a u_ba   (the prism)
+//   0 outside (g0 <= 0 < ga):      t_a0 + u_a0 (t_b0 + u_b0 t_70)
+// -- non-negative terms only, the same instructions on every lane, and the 19
+// edge reciprocals shared by the 6 tets.  A face function turns a value a
+// few ulps off its exact one, so a plane passing close to a corner keeps its
+// relative precision.
+ADECO_HD inline float halfspace_cube_vol6(F2 G0, float nx, float ny, float nz)
 {
-    const F2 g1 = f2_add(G0, F2{nx, 0.f}), g2 = f2_add(G0, F2{ny, 0.f}), g4 = f2_add(G0, F2{nz, 0.f});
-    const F2 g3 = f2_add(g1, F2{ny, 0.f}), g5 = f2_add(g1, F2{nz, 0.f}), g6 = f2_add(g2, F2{nz, 0.f});
-    const F2 g7 = f2_add(g3, F2{nz, 0.f});
-    P[0] = G0.hi + G0.lo;
-    P[1] = g1.hi;
-    P[2] = g2.hi;
-    P[3] = g3.hi;
-    P[4] = g4.hi;
-    P[5] = g5.hi;
-    P[6] = g6.hi;
-    P[7] = g7.hi;
-}
-
-// 6x volume of the unit cube's part where G > 0, from G's values at the 8
-// corners: the cube is split into the 6 tets around its diagonal
-// (0,0,0)-(1,1,1), each of 6x volume 1, and each tet's inside fraction comes
-// from G's values at its vertices -- non-negative terms only, so no
-// cancellation, and the same arithmetic for every lane.
-ADECO_HD inline float halfspace_cube_vol6(const float G[8])
-{
-    const int in0 = (int)(G[0] > 0.f), in7 = (int)(G[7] > 0.f);
-    const int path[6][2] = {{1, 3}, {1, 5}, {2, 3}, {2, 6}, {4, 5}, {4, 6}};
+    G0 = f2_add(G0, F2{fminf(nx, 0.f), 0.f});
+    G0 = f2_add(G0, F2{fminf(ny, 0.f), 0.f});
+    G0 = f2_add(G0, F2{fminf(nz, 0.f), 0.f});
+    nx = fabsf(nx);
+    ny = fabsf(ny);
+    nz = fabsf(nz);
+    const F2 e1 = f2_add(G0, F2{nx, 0.f}), e2 = f2_add(G0, F2{ny, 0.f}), e4 = f2_add(G0, F2{nz, 0.f});
+    const F2 e3 = f2_add(e1, F2{ny, 0.f}), e5 = f2_add(e1, F2{nz, 0.f}), e6 = f2_add(e2, F2{nz, 0.f});
+    const F2 e7 = f2_add(e3, F2{nz, 0.f});
+    const float g0 = G0.hi + G0.lo, g7 = e7.hi;
+    const float ga[3] = {e1.hi, e2.hi, e4.hi};  // a = 1, 2, 4
+    const float gb[3] = {e3.hi, e5.hi, e6.hi};  // b = 3, 5, 6
+    if (!(g7 > 0.f)) return 0.f;
+    if (g0 > 0.f) return 6.f;
+    const float r70 = rcp_nr(g7 - g0);
+    const float t70 = g7 * r70;
+    float ta0[3], ua0[3], t7a[3], tb0[3], ub0[3], t7b[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const float ra0 = rcp_nr(ga[i] - g0), rb0 = rcp_nr(gb[i] - g0);
+        ta0[i] = ga[i] * ra0;
+        ua0[i] = -g0 * ra0;
+        tb0[i] = gb[i] * rb0;
+        ub0[i] = -g0 * rb0;
+        t7a[i] = g7 * rcp_nr(g7 - ga[i]);
+        t7b[i] = g7 * rcp_nr(g7 - gb[i]);
+    }
+    // tets (a, b) by index into ga / gb: (1,3) (1,5) (2,3) (2,6) (4,5) (4,6)
+    const int ia[6] = {0, 0, 1, 1, 2, 2}, ib[6] = {0, 1, 0, 2, 1, 2};
     float v = 0.f;
 #pragma unroll
     for (int q = 0; q < 6; ++q) {
-        const float x1 = G[path[q][0]], x2 = G[path[q][1]];
-        const int mask = in0 | ((int)(x1 > 0.f) << 1) | ((int)(x2 > 0.f) << 2) | (in7 << 3);
-        v += (mask == 15) ? 1.f : ((mask == 0) ? 0.f : side_fraction(G[0], x1, x2, G[7], mask, 0.f));
+        const int i = ia[q], j = ib[q];
+        const float rba = rcp_nr(gb[j] - ga[i]);
+        const float tba = gb[j] * rba, uba = -ga[i] * rba;
+        const float k1 = t70 * t7a[i] * t7b[j];
+        const float k2 = fmaf(tb0[j], tba, t70 * fmaf(tba, ub0[j], t7a[i] * uba));
+        const float k3 = fmaf(ua0[i], fmaf(ub0[j], t70, tb0[j]), ta0[i]);
+        v += (gb[j] <= 0.f) ? k1 : ((ga[i] <= 0.f) ? k2 : k3);
     }
     return v;
 }

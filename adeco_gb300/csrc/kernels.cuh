@@ -613,9 +613,7 @@ inline
 #endif
 float halfspace_pair_vol6(const WarpTets &W, const GridDesc &g, int s, int a, int b, int c, int f)
 {
-    float P[8];
-    cube_corner_values(face_value_at_cell(W, g, s, a, b, c, f), W.n[f][0][s], W.n[f][1][s], W.n[f][2][s], P);
-    return halfspace_cube_vol6(P);
+    return halfspace_cube_vol6(face_value_at_cell(W, g, s, a, b, c, f), W.n[f][0][s], W.n[f][1][s], W.n[f][2][s]);
 }
 
 // Non-negative mass of a pair (FP32, about 1e-7 relative) -> the cell's
