@@ -416,11 +416,16 @@ F2 clip_bary_serial(const float *rec0, int done0)
 
 
 constexpr int kVolShift = 56;  // fixed point of 6x piece volumes (each <= 6)
+static_assert(kVolShift == 56, "vol_fixed scales by 0x1p56f");
 
 ADECO_HD inline long long vol_fixed(float v6)
 {
+#ifdef __CUDA_ARCH__
+    return __float2ll_rn(v6 * 0x1p56f);  // the signed form of to_fixed(|v6|, kVolShift)
+#else
     const unsigned long long m = to_fixed(fabsf(v6), kVolShift);
     return v6 < 0.f ? -(long long)m : (long long)m;
+#endif
 }
 
 ADECO_HD inline float piece_vol6(const float p[12])
