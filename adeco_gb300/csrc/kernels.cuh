@@ -236,6 +236,33 @@ __device__ __forceinline__ void load_tet(const float4 *vert, int vx, int vy, int
 // 27-bit local index); a larger tet sets the error flag and is skipped.
 constexpr long long kMaxPairsPerTet = 1LL << 25;
 
+// Offset of a tet face's plane n . x = d through the face's centroid, from
+// its vertices as FP32 pairs (hi + lo) and the FP32 normal n: 3 d = n . (va
+// + vb + vc) in double-float, divided by 3 as a product with 1/3 whose
+// remainder (exact, fma) is carried into the low part, so that d_hi + d_lo
+// keeps ~44 bits.
+ADECO_HD inline F2 plane_offset(const float qa[3], const float la[3], const float qb[3], const float lb[3],
+                                const float qc[3], const float lc[3], const float n[3])
+{
+    F2 dd = {0.f, 0.f};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const F2 sum = f2_add(f2_add(F2{qa[a], la[a]}, F2{qb[a], lb[a]}), F2{qc[a], lc[a]});
+        dd = f2_add(dd, f2_mul_f(sum, n[a]));
+    }
+    constexpr float kThird = 1.f / 3.f;
+    const float d_hi = dd.hi * kThird;
+    return {d_hi, (fmaf(-d_hi, 3.f, dd.hi) + dd.lo) * kThird};
+}
+
+// kExactD: store each face's exact plane offset (d, dlo: the one-face closed
+// form reads them).  Otherwise only an FP32 d for the classification, whose
+// error band covers its rounding; the closed form then forms the exact
+// offset itself (plane_offset from the stored vertices) for the few pairs
+// that take it.  Octree leaves at the benchmark's cell sizes send almost no
+// pair to the closed form, and the double-float offsets had been ~40% of the
+// set-up; zoom grids, fine against the tets, send many.
+template <bool kExactD = true>
 ADECO_HD inline int setup_tet(const float3 vin[4], const float ghin[4][3], const float glin[4][3], const GridDesc &g,
                               WarpTets &W, int lane, int *error, bool *fp64_route)
 {
@@ -301,9 +328,9 @@ ADECO_HD inline int setup_tet(const float3 vin[4], const float ghin[4][3], const
     const float f6 = f2_div_to_f(F2{g.mf_hi, g.mf_lo}, w6);  // mass per unit of 6x volume
     // planes from the FP32 vertices: inward normals (outward ones negated:
     // faces (0,1,2) (0,2,3) (0,3,1) (1,3,2)); each plane's offset is taken
-    // through the face's centroid, in double-float from the vertex pairs, so
-    // that the FP32 rounding of the normal only turns the plane about the
-    // centroid (the one-face closed form relies on it)
+    // through the face's centroid, so that the FP32 rounding of the normal
+    // only turns the plane about the centroid (the one-face closed form
+    // relies on it)
     const int fa[4] = {0, 0, 0, 1}, fb[4] = {2, 3, 1, 2}, fc[4] = {1, 2, 3, 3};
     float R = 0.f;
 #pragma unroll
@@ -321,23 +348,19 @@ ADECO_HD inline int setup_tet(const float3 vin[4], const float ghin[4][3], const
                     e2z = qf[fc[f]][2] - qf[fa[f]][2];
         const float nx = e1y * e2z - e1z * e2y, ny = e1z * e2x - e1x * e2z, nz = e1x * e2y - e1y * e2x;
         const float nn[3] = {nx, ny, nz};
-        F2 dd = {0.f, 0.f};  // 3 n . centroid = n . (va + vb + vc)
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            const F2 sum = f2_add(f2_add(F2{qf[fa[f]][a], ql[fa[f]][a]}, F2{qf[fb[f]][a], ql[fb[f]][a]}),
-                                  F2{qf[fc[f]][a], ql[fc[f]][a]});
-            dd = f2_add(dd, f2_mul_f(sum, nn[a]));
-        }
-        // / 3 as a product with 1/3: the remainder of d_hi is exact (fma) and
-        // carried into d_lo, so d_hi + d_lo keeps ~44 bits without a division
-        constexpr float kThird = 1.f / 3.f;
-        const float d_hi = dd.hi * kThird;
-        const float d_lo = (fmaf(-d_hi, 3.f, dd.hi) + dd.lo) * kThird;
         W.n[f][0][lane] = nx;
         W.n[f][1][lane] = ny;
         W.n[f][2][lane] = nz;
-        W.d[f][lane] = d_hi;
-        W.dlo[f][lane] = d_lo;
+        if (kExactD) {
+            const F2 d = plane_offset(qf[fa[f]], ql[fa[f]], qf[fb[f]], ql[fb[f]], qf[fc[f]], ql[fc[f]], nn);
+            W.d[f][lane] = d.hi;
+            W.dlo[f][lane] = d.lo;
+        } else {
+            constexpr float kThird = 1.f / 3.f;
+            W.d[f][lane] = (nx * (qf[fa[f]][0] + qf[fb[f]][0] + qf[fc[f]][0]) +
+                            ny * (qf[fa[f]][1] + qf[fb[f]][1] + qf[fc[f]][1]) +
+                            nz * (qf[fa[f]][2] + qf[fb[f]][2] + qf[fc[f]][2])) * kThird;
+        }
         const float L1 = fmaxf(fmaxf(fabsf(e1x), fabsf(e1y)), fabsf(e1z));
         const float L2 = fmaxf(fmaxf(fabsf(e2x), fabsf(e2y)), fabsf(e2z));
         // generous bound on the FP32 rounding of n.x - d (|x| <= R + 1)
@@ -590,10 +613,30 @@ ADECO_HD inline int classify_pair(const WarpTets &W, const GridDesc &g, int s, i
 // n . origin - (d + dlo) cancels terms as large as the tet is wide in cells:
 // it is formed exactly in double-float (TwoProd of n with the integer cell
 // offsets) and kept as a pair for the corner values.
+template <bool kExactD = true>
 ADECO_HD inline F2 face_value_at_cell(const WarpTets &W, const GridDesc &g, int s, int a, int b, int c, int f)
 {
     const int cc[3] = {a, b, c};
-    F2 G = {-W.d[f][s], -W.dlo[f][s]};
+    F2 G;
+    if (kExactD) {
+        G = {-W.d[f][s], -W.dlo[f][s]};
+    } else {  // the exact offset setup_tet<true> would have stored
+        const int fa = f == 3 ? 1 : 0, fb = f == 0 ? 2 : (f == 1 ? 3 : (f == 2 ? 1 : 2)),
+                  fc = f == 0 ? 1 : (f == 1 ? 2 : 3);
+        float q[3][3], l[3][3];
+#pragma unroll
+        for (int x = 0; x < 3; ++x) {
+            q[0][x] = W.q[3 * fa + x][s];
+            l[0][x] = W.qlo[3 * fa + x][s];
+            q[1][x] = W.q[3 * fb + x][s];
+            l[1][x] = W.qlo[3 * fb + x][s];
+            q[2][x] = W.q[3 * fc + x][s];
+            l[2][x] = W.qlo[3 * fc + x][s];
+        }
+        const float n[3] = {W.n[f][0][s], W.n[f][1][s], W.n[f][2][s]};
+        const F2 d = plane_offset(q[0], l[0], q[1], l[1], q[2], l[2], n);
+        G = {-d.hi, -d.lo};
+    }
     float small = 0.f;  // the cells' deviation from unit size: n_x c_x dr_x, tiny
 #pragma unroll
     for (int x = 0; x < 3; ++x) {
@@ -606,6 +649,7 @@ ADECO_HD inline F2 face_value_at_cell(const WarpTets &W, const GridDesc &g, int 
 
 // 6x volume of cell (a, b, c) ∩ slot s's tet when the cell straddles only
 // face f: the cube's part on its inside.
+template <bool kExactD = true>
 #ifdef __CUDA_ARCH__
 __device__ __noinline__
 #else
@@ -613,7 +657,8 @@ inline
 #endif
 float halfspace_pair_vol6(const WarpTets &W, const GridDesc &g, int s, int a, int b, int c, int f)
 {
-    return halfspace_cube_vol6(face_value_at_cell(W, g, s, a, b, c, f), W.n[f][0][s], W.n[f][1][s], W.n[f][2][s]);
+    return halfspace_cube_vol6(face_value_at_cell<kExactD>(W, g, s, a, b, c, f), W.n[f][0][s], W.n[f][1][s],
+                               W.n[f][2][s]);
 }
 
 // Non-negative mass of a pair (FP32, about 1e-7 relative) -> the cell's
@@ -721,6 +766,7 @@ struct PairStats {
 // Sets up group grp (tets 32 grp .. 32 grp + 31 of the item's live cubes) in
 // the warp's table W and returns its candidate pairs.  route64: this lane's
 // tet is ill-conditioned (listed by group_route, no pairs here).
+template <bool kShare>
 __device__ __forceinline__ int group_setup(const DepositParams &P, const SharedMixed &S, WarpTets &W,
                                            const GridDesc &g, int grp, int ntet, int vx, int vy, int cvx, int cvy,
                                            int lane, PairStats &st, bool &route64, int &tid)
@@ -740,7 +786,7 @@ __device__ __forceinline__ int group_setup(const DepositParams &P, const SharedM
                 gh[q][a] = S.gh[a][vid[q]];
                 gl[q][a] = S.gl[a][vid[q]];
             }
-        cnt = setup_tet(v, gh, gl, g, W, lane, P.error, &route64);
+        cnt = setup_tet<kShare>(v, gh, gl, g, W, lane, P.error, &route64);
     }
     st.tets += (cnt > 0);
     route64 = route64 && cnt > 0;
@@ -777,6 +823,7 @@ __device__ __forceinline__ void group_route(const DepositParams &P, const Shared
 // warp: classified, inside cells and one-face cells deposited at once,
 // partial cells listed in Q and clipped by the engine (one call site keeps a
 // single copy of it).
+template <bool kShare>
 __device__ __forceinline__ void pair_range(const DepositParams &P, const GridDesc &g, const WarpTets &Wc,
                                            WarpPool &pool, uint32_t *Q, int c0, int c1, int lane, PairStats &st)
 {
@@ -817,7 +864,7 @@ __device__ __forceinline__ void pair_range(const DepositParams &P, const GridDes
                 ++st.part;
                 ++st.bbox;
                 if (cross >= 0) {  // one face cuts the cell: closed form, no clipping
-                    const float dm = halfspace_pair_vol6(Wc, g, s, a, b, c, cross) * Wc.f6[s];
+                    const float dm = halfspace_pair_vol6<kShare>(Wc, g, s, a, b, c, cross) * Wc.f6[s];
                     if (dm > 0.f) scatter(P, g, Wc, s, a, b, c, dm);
                 } else {
                     part = true;
@@ -895,8 +942,8 @@ __global__ void __launch_bounds__(kThreads, 2) deposit_mixed_kernel(DepositParam
                 if (grp >= ngroups) break;
                 bool route64;
                 int tid;
-                const int total = group_setup(P, S, W, g, grp, ntet, vx, vy, cvx, cvy, lane, st, route64, tid);
-                pair_range(P, g, W, pool, Q, 0, total, lane, st);
+                const int total = group_setup<kShare>(P, S, W, g, grp, ntet, vx, vy, cvx, cvy, lane, st, route64, tid);
+                pair_range<kShare>(P, g, W, pool, Q, 0, total, lane, st);
                 group_route(P, S, item, route64, tid);
                 __syncwarp();
             }
@@ -912,7 +959,7 @@ __global__ void __launch_bounds__(kThreads, 2) deposit_mixed_kernel(DepositParam
                     if (grp < ngroups) {
                         bool route64;
                         int tid;
-                        total = group_setup(P, S, W, g, grp, ntet, vx, vy, cvx, cvy, lane, st, route64, tid);
+                        total = group_setup<kShare>(P, S, W, g, grp, ntet, vx, vy, cvx, cvy, lane, st, route64, tid);
                         group_route(P, S, item, route64, tid);
                         // a group of one chunk or less is kept private
                         const bool pub = total > chunk;
@@ -989,7 +1036,7 @@ __global__ void __launch_bounds__(kThreads, 2) deposit_mixed_kernel(DepositParam
                     cur = -1;
                     continue;
                 }
-                pair_range(P, g, S.wt[cur], pool, Q, c0, min(total, c0 + chunk), lane, st);
+                pair_range<kShare>(P, g, S.wt[cur], pool, Q, c0, min(total, c0 + chunk), lane, st);
             }
         }
         __syncthreads();
