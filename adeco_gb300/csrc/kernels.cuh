@@ -1241,11 +1241,14 @@ __device__ __forceinline__ int route_classify(const RouteTet &T, const GridDesc 
 }
 
 // Clip the np partial cells listed in RW.pool (local indices a + ex0 (b +
-// ex1 k)) with the barycentric warp engine and deposit their masses.  One
-// copy of the engine, called from every place a list fills.
-__device__ __noinline__ void route_flush(RouteWarp &RW, const GridDesc &g, const int lo[3], int np,
-                                         unsigned long long *out, unsigned &fallbacks)
+// ex1 k)) with the barycentric warp engine and deposit their masses; returns
+// the pieces clipped serially.  One copy of the engine, called from every
+// place a list fills.  Arguments by value: a reference to a caller's local
+// variable would put it in local memory.
+__device__ __noinline__ unsigned route_flush(RouteWarp &RW, const GridDesc &g, int lo0, int lo1, int lo2, int np,
+                                             unsigned long long *out)
 {
+    unsigned fallbacks = 0;
     const int lane = threadIdx.x & 31;
     const RouteTet &T = RW.t;
     BaryPool &pool = RW.pool;
@@ -1278,10 +1281,11 @@ __device__ __noinline__ void route_flush(RouteWarp &RW, const GridDesc &g, const
         const double dm = ldexp((double)pool.acc[j], -kVolShift) * g.mass_factor;
         const unsigned long long fx = (unsigned long long)llrint(ldexp(dm, g.shift));
         if (dm > 0.0 && fx)
-            atomicAdd(out + g.out_offset + (lo[0] + a) + (long long)g.dims * ((lo[1] + b) + (long long)g.dims * (lo[2] + k)),
+            atomicAdd(out + g.out_offset + (lo0 + a) + (long long)g.dims * ((lo1 + b) + (long long)g.dims * (lo2 + k)),
                       fx);
     }
     __syncwarp();
+    return fallbacks;
 }
 
 // One ill-conditioned tet, candidate range [lo, hi], deposited by a warp.
@@ -1293,9 +1297,9 @@ __device__ __noinline__ void route_flush(RouteWarp &RW, const GridDesc &g, const
 // or inside it are deposited at once; partial cells are listed and, 32 or
 // more at a time, clipped by the barycentric warp engine from the FP32 hi +
 // lo cell coordinates: the share of the tet times its exact mass.
-__device__ __noinline__ void route_tet_warp(const float3 v[4], const int lo[3], const int hi[3], const GridDesc &g,
-                                            unsigned long long *out, RouteWarp &RW, unsigned &n_cand, unsigned &n_part,
-                                            unsigned &n64, unsigned &fallbacks)
+__device__ __forceinline__ void route_tet_warp(const float3 v[4], const int lo[3], const int hi[3], const GridDesc &g,
+                                               unsigned long long *out, RouteWarp &RW, unsigned &n_cand,
+                                               unsigned &n_part, unsigned &n64, unsigned &fallbacks)
 {
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1;
@@ -1315,7 +1319,7 @@ __device__ __noinline__ void route_tet_warp(const float3 v[4], const int lo[3], 
     };
     int np = 0;  // listed partial cells (the same in every lane)
     auto flush = [&]() {
-        route_flush(RW, g, lo, np, out, fallbacks);
+        fallbacks += route_flush(RW, g, lo[0], lo[1], lo[2], np, out);
         np = 0;
     };
     auto offer = [&](bool has, int a, int b, int k) {
@@ -1414,6 +1418,9 @@ __device__ __noinline__ void route_tet_warp(const float3 v[4], const int lo[3], 
 
 // The tets deposit_mixed_kernel listed (kappa > kKappaFp64), one warp each:
 // vertices re-read from the source, then route_tet_warp.
+// Two CTAs of 8 warps per SM.  The barycentric engine's 28-float pieces
+// would need ~220 registers a thread and spill some at 128; one CTA per SM
+// without spills was slower (a 256^3 clustered lattice: 696 against 636 ms).
 __global__ void __launch_bounds__(kThreads, 2) route_fp64_kernel(DepositParams P)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];

@@ -233,7 +233,7 @@ int launch_mixed(const DeviceProps &dp, DepositParams P, bool share, cudaStream_
     else
         deposit_mixed_kernel<false><<<grid, kThreads, dp.mixed_smem, st>>>(P);
     CUDA_TRY(cudaGetLastError());
-    route_fp64_kernel<<<dp.sms * 4, kThreads, kRouteSmem, st>>>(P);
+    route_fp64_kernel<<<dp.sms * 2, kThreads, kRouteSmem, st>>>(P);  // the resident CTAs
     CUDA_TRY(cudaGetLastError());
     return ADECO_OK;
 }
@@ -1449,7 +1449,7 @@ extern "C" int adeco_deposit_tets_device_noalloc(const float *d_positions, size_
     const int blocks = (int)std::max(1LL, std::min(n_items, (long long)nd.sms * nd.blocks_per_sm));
     deposit_mixed_kernel<false><<<blocks, kThreads, sizeof(SharedMixed), st>>>(P);
     CUDA_TRY(cudaGetLastError());
-    route_fp64_kernel<<<nd.sms * 4, kThreads, kRouteSmem, st>>>(P);
+    route_fp64_kernel<<<nd.sms * 2, kThreads, kRouteSmem, st>>>(P);  // the resident CTAs
     CUDA_TRY(cudaGetLastError());
     fixed_accumulate_f64_kernel<<<1024, 256, 0, st>>>(fixed, d_out, ncell, std::ldexp(1.0, -shift));
     CUDA_TRY(cudaGetLastError());
