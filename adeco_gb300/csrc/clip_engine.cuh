@@ -335,6 +335,73 @@ ADECO_HD inline F2 bary_share(const float *w)
 
 constexpr int kBaryRec = 28;  // a barycentric piece: 16 weights (4 per vertex), then 12 coordinates
 
+// record entry of vertex v's value i (0..3 weights, 4..6 coordinates)
+ADECO_HD inline int bary_idx(int v, int i) { return i < 4 ? 4 * v + i : 16 + 3 * v + (i - 4); }
+
+// Split of barycentric piece r by face f (mask: its vertices inside, k of
+// them), with split_cut's patterns over the 7 values of a vertex: the
+// vertices permuted to A B C D (inside first, even permutation), the cut
+// points E0..E3 of the edges k=1: AB AC AD AD; k=2: AC AD BC BD; k=3: AD BD CD
+// CD (weights interpolated with the coordinate's edge parameter, the
+// coordinate snapped onto the face), and the children
+//   c0 = (A, k1 ? E0 : B, k1 ? E1 : (k2 ? E2 : C), k1 ? E2 : (k2 ? E3 : E2))
+//   c1 = (A, k2 ? E2 : B, k2 ? E0 : E2, k2 ? E3 : E1)
+//   c2 = (A, k2 ? E0 : E1, k2 ? E1 : E2, k2 ? E3 : E0)
+// written entry by entry as put(child, record index, value): each child
+// vertex is a select between at most three candidates, no lookup.  Returns
+// the number of children (1 or 3).
+template <typename Put>
+ADECO_HD inline int bary_split(const float *r, int f, int mask, Put put)
+{
+    const int axis = f >> 1;
+    const float plane = (f & 1) ? 1.f : 0.f;
+    const int pm = split_perm(mask), k = split_kin(mask);
+    const bool k1 = k == 1, k2 = k == 2, k3 = k == 3;
+    const int ia = pm & 3, ib = (pm >> 2) & 3, ic = (pm >> 4) & 3, id = (pm >> 6) & 3;
+    float A[7], B[7], C[7], D[7];
+#pragma unroll
+    for (int i = 0; i < 7; ++i) {
+        const float a0 = r[bary_idx(0, i)], a1 = r[bary_idx(1, i)], a2 = r[bary_idx(2, i)], a3 = r[bary_idx(3, i)];
+        A[i] = sel4(ia, a0, a1, a2, a3);
+        B[i] = sel4(ib, a0, a1, a2, a3);
+        C[i] = sel4(ic, a0, a1, a2, a3);
+        D[i] = sel4(id, a0, a1, a2, a3);
+    }
+    float E[4][7];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        float in[7], out[7];
+#pragma unroll
+        for (int i = 0; i < 7; ++i) {
+            in[i] = e == 0 ? A[i] : (e == 1 ? (k3 ? B[i] : A[i]) : (e == 2 ? (k1 ? A[i] : (k2 ? B[i] : C[i]))
+                                                                             : (k2 ? B[i] : (k3 ? C[i] : A[i]))));
+            out[i] = e == 0 ? (k1 ? B[i] : (k2 ? C[i] : D[i])) : (e == 1 ? (k1 ? C[i] : D[i])
+                                                                          : (e == 2 ? (k2 ? C[i] : D[i]) : D[i]));
+        }
+        const float xin = sel3(axis, in[4], in[5], in[6]), xout = sel3(axis, out[4], out[5], out[6]);
+        const float t = fminf(fmaxf((plane - xin) * rcp_nr(xout - xin), 0.f), 1.f);
+#pragma unroll
+        for (int i = 0; i < 7; ++i) E[e][i] = (i == 4 + axis) ? plane : fmaf(t, out[i] - in[i], in[i]);
+    }
+#pragma unroll
+    for (int i = 0; i < 7; ++i) {
+        put(0, bary_idx(0, i), A[i]);
+        put(0, bary_idx(1, i), k1 ? E[0][i] : B[i]);
+        put(0, bary_idx(2, i), k1 ? E[1][i] : (k2 ? E[2][i] : C[i]));
+        put(0, bary_idx(3, i), k1 ? E[2][i] : (k2 ? E[3][i] : E[2][i]));
+        put(1, bary_idx(0, i), A[i]);
+        put(1, bary_idx(1, i), k2 ? E[2][i] : B[i]);
+        put(1, bary_idx(2, i), k2 ? E[0][i] : E[2][i]);
+        put(1, bary_idx(3, i), k2 ? E[3][i] : E[1][i]);
+        put(2, bary_idx(0, i), A[i]);
+        put(2, bary_idx(1, i), k2 ? E[0][i] : E[1][i]);
+        put(2, bary_idx(2, i), k2 ? E[1][i] : E[2][i]);
+        put(2, bary_idx(3, i), k2 ? E[3][i] : E[0][i]);
+    }
+    return k1 ? 1 : 3;
+}
+
+
 // The share inside the unit cube of one barycentric piece rec0 whose faces
 // in done0 are already done, clipped serially with a stack.
 ADECO_HD
@@ -376,37 +443,13 @@ F2 clip_bary_serial(const float *rec0, int done0)
             acc = f2_add(acc, f2_mul_f(bary_share(w), side_fraction(xa[0], xa[1], xa[2], xa[3], mask, plane)));
             continue;
         }
-        // split by face f into 1 or 3 pieces (vertex patterns of split_cut)
-        const int pm = split_perm(mask), k = split_kin(mask);
-        const int id[4] = {pm & 3, (pm >> 2) & 3, (pm >> 4) & 3, (pm >> 6) & 3};
-        // edges: k=1: AB AC AD; k=2: AC AD BC BD; k=3: AD BD CD
-        const int ein[4] = {0, (k == 3) ? 1 : 0, (k == 1) ? 0 : ((k == 2) ? 1 : 2), 1};
-        const int eout[4] = {(k == 1) ? 1 : ((k == 2) ? 2 : 3), (k == 1) ? 2 : 3, (k == 2) ? 2 : 3, 3};
-        float E[4][7];  // cut points: 4 weights + 3 coordinates
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-            const int vi = id[ein[e]], vo = id[eout[e]];
-            const float t = fminf(fmaxf((plane - xa[vi]) / (xa[vo] - xa[vi]), 0.f), 1.f);
-#pragma unroll
-            for (int i = 0; i < 4; ++i) E[e][i] = fmaf(t, w[4 * vo + i] - w[4 * vi + i], w[4 * vi + i]);
-#pragma unroll
-            for (int a = 0; a < 3; ++a)
-                E[e][4 + a] = (a == axis) ? plane : fmaf(t, x[3 * vo + a] - x[3 * vi + a], x[3 * vi + a]);
-        }
-        // children as vertex lists: indices 0..3 = A..D (permuted), 4..7 = E0..E3
-        const int ch[3][4] = {{0, k == 1 ? 4 : 1, k == 1 ? 5 : (k == 2 ? 6 : 2), k == 1 ? 6 : (k == 2 ? 7 : 6)},
-                              {0, k == 2 ? 6 : 1, k == 2 ? 4 : 6, k == 2 ? 7 : 5},
-                              {0, k == 2 ? 4 : 5, k == 2 ? 5 : 6, k == 2 ? 7 : 4}};
-        const int n = (k == 1) ? 1 : 3;
+        // split by face f into 1 or 3 pieces (bary_split, as the warp engine)
+        const int n = split_kin(mask) == 1 ? 1 : 3;
         if (sp + n > kDepth) continue;  // cannot happen: at most 2 pending pieces per face level
+        bary_split(r, f, mask, [&](int ch, int e, float val) {
+            if (ch < n) stk[sp + ch][e] = val;
+        });
         for (int c = 0; c < n; ++c) {
-            for (int v = 0; v < 4; ++v) {
-                const int src = ch[c][v];
-#pragma unroll
-                for (int i = 0; i < 4; ++i) stk[sp][4 * v + i] = (src < 4) ? w[4 * id[src] + i] : E[src - 4][i];
-#pragma unroll
-                for (int a = 0; a < 3; ++a) stk[sp][16 + 3 * v + a] = (src < 4) ? x[3 * id[src] + a] : E[src - 4][4 + a];
-            }
             sdone[sp] = done | (1 << f);
             ++sp;
         }
@@ -642,11 +685,6 @@ struct BaryPool {
     uint32_t cell[kBaryList];  // the listed cells (the caller's encoding)
 };
 
-// value i (0..3 weights, 4..6 coordinates) of vertex v of a record
-__device__ __forceinline__ float bary_val(const float *r, int v, int i)
-{
-    return i < 4 ? r[4 * v + i] : r[16 + 3 * v + (i - 4)];
-}
 
 // next_face of a barycentric piece whose faces in `done` are done
 __device__ __forceinline__ int bary_step(const float *r, int done, int &face, int &mask, bool &last)
@@ -661,63 +699,6 @@ __device__ __forceinline__ float bary_last_fraction(const float *r, int f, int m
     const float plane = (f & 1) ? 1.f : 0.f;
     return side_fraction(sel3(axis, r[16], r[17], r[18]), sel3(axis, r[19], r[20], r[21]),
                          sel3(axis, r[22], r[23], r[24]), sel3(axis, r[25], r[26], r[27]), mask, plane);
-}
-
-// split at face f: P = the vertices in split_perm order (inside first), E =
-// the cut points of the k-pattern's edges (k=1: AB AC AD; k=2: AC AD BC BD;
-// k=3: AD BD CD), each 4 weights + 3 coordinates
-__device__ __forceinline__ void bary_split(const float *r, int f, int mask, float P[4][7], float E[4][7], int &k)
-{
-    const int pm = split_perm(mask);
-    k = split_kin(mask);
-    const int id0 = pm & 3, id1 = (pm >> 2) & 3, id2 = (pm >> 4) & 3, id3 = (pm >> 6) & 3;
-#pragma unroll
-    for (int i = 0; i < 7; ++i) {
-        const float a0 = bary_val(r, 0, i), a1 = bary_val(r, 1, i), a2 = bary_val(r, 2, i), a3 = bary_val(r, 3, i);
-        P[0][i] = sel4(id0, a0, a1, a2, a3);
-        P[1][i] = sel4(id1, a0, a1, a2, a3);
-        P[2][i] = sel4(id2, a0, a1, a2, a3);
-        P[3][i] = sel4(id3, a0, a1, a2, a3);
-    }
-    const int axis = f >> 1;
-    const float plane = (f & 1) ? 1.f : 0.f;
-#pragma unroll
-    for (int e = 0; e < 4; ++e) {
-        const int vi = e == 0 ? 0 : (e == 1 ? (k == 3 ? 1 : 0) : (e == 2 ? (k == 1 ? 0 : (k == 2 ? 1 : 2)) : 1));
-        const int vo = e == 0 ? (k == 1 ? 1 : (k == 2 ? 2 : 3))
-                              : (e == 1 ? (k == 1 ? 2 : 3) : (e == 2 ? (k == 2 ? 2 : 3) : 3));
-        float pin[7], pout[7];
-#pragma unroll
-        for (int i = 0; i < 7; ++i) {
-            pin[i] = sel4(vi, P[0][i], P[1][i], P[2][i], P[3][i]);
-            pout[i] = sel4(vo, P[0][i], P[1][i], P[2][i], P[3][i]);
-        }
-        const float xin = sel3(axis, pin[4], pin[5], pin[6]), xout = sel3(axis, pout[4], pout[5], pout[6]);
-        const float t = fminf(fmaxf((plane - xin) / (xout - xin), 0.f), 1.f);
-#pragma unroll
-        for (int i = 0; i < 4; ++i) E[e][i] = fmaf(t, pout[i] - pin[i], pin[i]);
-#pragma unroll
-        for (int a = 0; a < 3; ++a) E[e][4 + a] = (a == axis) ? plane : fmaf(t, pout[4 + a] - pin[4 + a], pin[4 + a]);
-    }
-}
-
-// vertex v of child c (0..3: P, 4..7: E) for pattern k: clip_bary_serial's table
-__device__ __forceinline__ int bary_src(int k, int c, int v)
-{
-    if (v == 0) return 0;
-    if (c == 0)
-        return v == 1 ? (k == 1 ? 4 : 1) : (v == 2 ? (k == 1 ? 5 : (k == 2 ? 6 : 2)) : (k == 1 ? 6 : (k == 2 ? 7 : 6)));
-    if (c == 1) return v == 1 ? (k == 2 ? 6 : 1) : (v == 2 ? (k == 2 ? 4 : 6) : (k == 2 ? 7 : 5));
-    return v == 1 ? (k == 2 ? 4 : 5) : (v == 2 ? (k == 2 ? 5 : 6) : (k == 2 ? 7 : 4));
-}
-
-// record entry x (0..27) of child c
-__device__ __forceinline__ float bary_child(const float P[4][7], const float E[4][7], int k, int c, int x)
-{
-    const int v = x < 16 ? x >> 2 : (x - 16) / 3;
-    const int i = x < 16 ? (x & 3) : 4 + (x - 16) % 3;
-    const int s = bary_src(k, c, v);
-    return s < 4 ? sel4(s, P[0][i], P[1][i], P[2][i], P[3][i]) : sel4(s - 4, E[0][i], E[1][i], E[2][i], E[3][i]);
 }
 
 __device__ __forceinline__ long long share_fixed(F2 c)
@@ -783,23 +764,19 @@ __device__ __forceinline__ void clip_bary_pairs(BaryPool &pool, int np, Build bu
         const bool defer = push && prank >= fit;
         const int nfit = min(__popc(pushing), fit);
         const bool stuck = held == 0xffffffffu && pushing == 0xffffffffu && fit == 0;
-        int k = 1;
-        bool split = false;
-        float P[4][7], E[4][7];
         if (valid && !defer) {
             F2 c = {0.f, 0.f};
             if (want_split) {
-                bary_split(r, f, mask, P, E, k);
-                split = true;
+                // the children of r: the first replaces r, the others go to
+                // the pool (written after every entry of r has been read)
+                const int base = top + 2 * prank;
+                bary_split(r, f, mask, [&](int ch, int x, float val) {
+                    if (ch == 0) r[x] = val;  // after bary_split's last read of r
+                    else if (push) pool.v[x][base + ch - 1] = val;
+                });
                 done |= 1 << f;
                 if (push) {
-                    const int base = top + 2 * prank;
                     const uint32_t m = (uint32_t)owner | ((uint32_t)done << 8);
-#pragma unroll
-                    for (int x = 0; x < kBaryRec; ++x) {
-                        pool.v[x][base] = bary_child(P, E, k, 1, x);
-                        pool.v[x][base + 1] = bary_child(P, E, k, 2, x);
-                    }
                     pool.meta[base] = m;
                     pool.meta[base + 1] = m;
                 }
@@ -820,10 +797,6 @@ __device__ __forceinline__ void clip_bary_pairs(BaryPool &pool, int np, Build bu
             ++fallbacks;
         }
         top += 2 * nfit;
-        if (split) {
-#pragma unroll
-            for (int x = 0; x < kBaryRec; ++x) r[x] = bary_child(P, E, k, 0, x);
-        }
         __syncwarp();
     }
     __syncwarp();
