@@ -315,8 +315,10 @@ ADECO_HD inline int next_face(int b0, int b1, int b2, int b3, int done, int &fac
 // order are the engine's, on the piece's own coordinates.
 
 // A piece's signed share of the tet: the determinant of its weight
-// differences (weights 1..3 of vertices 1..3 minus those of vertex 0), from
-// exact differences in double-float.  Signed: every piece keeps the tet's
+// differences (the weights of vertices 1..3 minus those of vertex 0), from
+// exact differences in double-float.  A record carries a vertex's weights
+// of tet vertices 1..3 only: the weight of vertex 0 (one minus their sum)
+// does not enter the determinant.  Signed: every piece keeps the tet's
 // orientation, and |det| would round near-degenerate pieces up and bias the
 // sum.
 ADECO_HD inline F2 bary_share(const float *w)
@@ -325,7 +327,7 @@ ADECO_HD inline F2 bary_share(const float *w)
 #pragma unroll
     for (int j = 0; j < 3; ++j)
 #pragma unroll
-        for (int i = 0; i < 3; ++i) d[j][i] = f2_two_sum(w[4 * (j + 1) + i + 1], -w[i + 1]);
+        for (int i = 0; i < 3; ++i) d[j][i] = f2_two_sum(w[3 * (j + 1) + i], -w[i]);
     const F2 m0 = f2_minor(d[1][1], d[2][2], d[1][2], d[2][1]);
     const F2 m1 = f2_minor(d[1][0], d[2][2], d[1][2], d[2][0]);
     const F2 m2 = f2_minor(d[1][0], d[2][1], d[1][1], d[2][0]);
@@ -333,13 +335,20 @@ ADECO_HD inline F2 bary_share(const float *w)
     return f2_add(f2_add(f2_mul(d[0][0], m0), {-t1.hi, -t1.lo}), f2_mul(d[0][2], m2));
 }
 
-constexpr int kBaryRec = 28;  // a barycentric piece: 16 weights (4 per vertex), then 12 coordinates
+constexpr int kBaryRec = 24;  // a barycentric piece: 12 weights (3 per vertex), then 12 coordinates
 
-// record entry of vertex v's value i (0..3 weights, 4..6 coordinates)
-ADECO_HD inline int bary_idx(int v, int i) { return i < 4 ? 4 * v + i : 16 + 3 * v + (i - 4); }
+// the tet itself: vertex v (1..3) has weight 1 for tet vertex v, vertex 0 none
+ADECO_HD inline void bary_identity(float *r)
+{
+#pragma unroll
+    for (int i = 0; i < 12; ++i) r[i] = (i & 3) == 3 ? 1.f : 0.f;  // entries 3, 7, 11
+}
+
+// record entry of vertex v's value i (0..2 weights, 3..5 coordinates)
+ADECO_HD inline int bary_idx(int v, int i) { return i < 3 ? 3 * v + i : 12 + 3 * v + (i - 3); }
 
 // Split of barycentric piece r by face f (mask: its vertices inside, k of
-// them), with split_cut's patterns over the 7 values of a vertex: the
+// them), with split_cut's patterns over the 6 values of a vertex: the
 // vertices permuted to A B C D (inside first, even permutation), the cut
 // points E0..E3 of the edges k=1: AB AC AD AD; k=2: AC AD BC BD; k=3: AD BD CD
 // CD (weights interpolated with the coordinate's edge parameter, the
@@ -358,33 +367,33 @@ ADECO_HD inline int bary_split(const float *r, int f, int mask, Put put)
     const int pm = split_perm(mask), k = split_kin(mask);
     const bool k1 = k == 1, k2 = k == 2, k3 = k == 3;
     const int ia = pm & 3, ib = (pm >> 2) & 3, ic = (pm >> 4) & 3, id = (pm >> 6) & 3;
-    float A[7], B[7], C[7], D[7];
+    float A[6], B[6], C[6], D[6];
 #pragma unroll
-    for (int i = 0; i < 7; ++i) {
+    for (int i = 0; i < 6; ++i) {
         const float a0 = r[bary_idx(0, i)], a1 = r[bary_idx(1, i)], a2 = r[bary_idx(2, i)], a3 = r[bary_idx(3, i)];
         A[i] = sel4(ia, a0, a1, a2, a3);
         B[i] = sel4(ib, a0, a1, a2, a3);
         C[i] = sel4(ic, a0, a1, a2, a3);
         D[i] = sel4(id, a0, a1, a2, a3);
     }
-    float E[4][7];
+    float E[4][6];
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
-        float in[7], out[7];
+        float in[6], out[6];
 #pragma unroll
-        for (int i = 0; i < 7; ++i) {
+        for (int i = 0; i < 6; ++i) {
             in[i] = e == 0 ? A[i] : (e == 1 ? (k3 ? B[i] : A[i]) : (e == 2 ? (k1 ? A[i] : (k2 ? B[i] : C[i]))
                                                                              : (k2 ? B[i] : (k3 ? C[i] : A[i]))));
             out[i] = e == 0 ? (k1 ? B[i] : (k2 ? C[i] : D[i])) : (e == 1 ? (k1 ? C[i] : D[i])
                                                                           : (e == 2 ? (k2 ? C[i] : D[i]) : D[i]));
         }
-        const float xin = sel3(axis, in[4], in[5], in[6]), xout = sel3(axis, out[4], out[5], out[6]);
+        const float xin = sel3(axis, in[3], in[4], in[5]), xout = sel3(axis, out[3], out[4], out[5]);
         const float t = fminf(fmaxf((plane - xin) * rcp_nr(xout - xin), 0.f), 1.f);
 #pragma unroll
-        for (int i = 0; i < 7; ++i) E[e][i] = (i == 4 + axis) ? plane : fmaf(t, out[i] - in[i], in[i]);
+        for (int i = 0; i < 6; ++i) E[e][i] = (i == 3 + axis) ? plane : fmaf(t, out[i] - in[i], in[i]);
     }
 #pragma unroll
-    for (int i = 0; i < 7; ++i) {
+    for (int i = 0; i < 6; ++i) {
         put(0, bary_idx(0, i), A[i]);
         put(0, bary_idx(1, i), k1 ? E[0][i] : B[i]);
         put(0, bary_idx(2, i), k1 ? E[1][i] : (k2 ? E[2][i] : C[i]));
@@ -425,7 +434,7 @@ F2 clip_bary_serial(const float *rec0, int done0)
         float r[kRec];
 #pragma unroll
         for (int i = 0; i < kRec; ++i) r[i] = stk[sp][i];
-        const float *w = r, *x = r + 16;
+        const float *w = r, *x = r + 12;
         const int done = sdone[sp];
         int f = 0, mask = 0;
         bool last = false;
@@ -689,16 +698,16 @@ struct BaryPool {
 // next_face of a barycentric piece whose faces in `done` are done
 __device__ __forceinline__ int bary_step(const float *r, int done, int &face, int &mask, bool &last)
 {
-    return next_face(face_bits(r[16], r[17], r[18]), face_bits(r[19], r[20], r[21]), face_bits(r[22], r[23], r[24]),
-                     face_bits(r[25], r[26], r[27]), done, face, mask, last);
+    return next_face(face_bits(r[12], r[13], r[14]), face_bits(r[15], r[16], r[17]), face_bits(r[18], r[19], r[20]),
+                     face_bits(r[21], r[22], r[23]), done, face, mask, last);
 }
 
 __device__ __forceinline__ float bary_last_fraction(const float *r, int f, int mask)
 {
     const int axis = f >> 1;
     const float plane = (f & 1) ? 1.f : 0.f;
-    return side_fraction(sel3(axis, r[16], r[17], r[18]), sel3(axis, r[19], r[20], r[21]),
-                         sel3(axis, r[22], r[23], r[24]), sel3(axis, r[25], r[26], r[27]), mask, plane);
+    return side_fraction(sel3(axis, r[12], r[13], r[14]), sel3(axis, r[15], r[16], r[17]),
+                         sel3(axis, r[18], r[19], r[20]), sel3(axis, r[21], r[22], r[23]), mask, plane);
 }
 
 __device__ __forceinline__ long long share_fixed(F2 c)

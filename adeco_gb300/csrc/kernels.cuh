@@ -1260,7 +1260,7 @@ __device__ __noinline__ unsigned route_flush(RouteWarp &RW, const GridDesc &g, i
             const int a = (int)(c % (uint32_t)ex0), rr = (int)(c / (uint32_t)ex0);
             const int b = rr % ex1, k = rr / ex1;
 #pragma unroll
-            for (int i = 0; i < 16; ++i) r[i] = (i % 5 == 0) ? 1.f : 0.f;
+            bary_identity(r);
             // coordinates in the cell's mirrored frame along axes whose lower
             // face the tet does not reach (as pair_piece); the shares come
             // from the weights, so no reordering is needed
@@ -1270,7 +1270,7 @@ __device__ __noinline__ unsigned route_flush(RouteWarp &RW, const GridDesc &g, i
                 const bool flip = T.bmin[x] > (float)cc[x];
 #pragma unroll
                 for (int q = 0; q < 4; ++q)
-                    r[16 + 3 * q + x] = cell_coord_sel(T.qf[q][x], T.ql[q][x], cc[x], g.drcell[x], flip);
+                    r[12 + 3 * q + x] = cell_coord_sel(T.qf[q][x], T.ql[q][x], cc[x], g.drcell[x], flip);
             }
         },
         fallbacks);
@@ -1418,9 +1418,10 @@ __device__ __forceinline__ void route_tet_warp(const float3 v[4], const int lo[3
 
 // The tets deposit_mixed_kernel listed (kappa > kKappaFp64), one warp each:
 // vertices re-read from the source, then route_tet_warp.
-// Two CTAs of 8 warps per SM.  The barycentric engine's 28-float pieces
-// would need ~220 registers a thread and spill some at 128; one CTA per SM
-// without spills was slower (a 256^3 clustered lattice: 696 against 636 ms).
+// Two CTAs of 8 warps per SM (128 registers a thread): with 28-float pieces
+// the engine spilled in its inner loop, and one CTA per SM without spills
+// (~220 registers) was slower still (a 256^3 clustered lattice: 696 against
+// 636 ms); its 24-float pieces now spill almost nothing.
 __global__ void __launch_bounds__(kThreads, 2) route_fp64_kernel(DepositParams P)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];

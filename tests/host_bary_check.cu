@@ -77,11 +77,11 @@ int main()
                     const double ref = clip_volume6<double, double>(P) / v6;
                     if (ref <= 0.0) continue;
                     float rec[kBaryRec], X[4][3];
-                    for (int m = 0; m < 16; ++m) rec[m] = (m % 5 == 0) ? 1.f : 0.f;
+                    bary_identity(rec);
                     for (int a = 0; a < 3; ++a) {
                         const bool flip = bmin[a] > (float)cc[a];
                         for (int q = 0; q < 4; ++q) {
-                            rec[16 + 3 * q + a] = cell_coord_sel(qf[q][a], ql[q][a], cc[a], 0.f, flip);
+                            rec[12 + 3 * q + a] = cell_coord_sel(qf[q][a], ql[q][a], cc[a], 0.f, flip);
                             X[q][a] = cell_coord(qf[q][a], ql[q][a], cc[a], 0.f);
                         }
                     }
