@@ -684,7 +684,7 @@ __device__ __forceinline__ void clip_pairs(WarpPool &pool, int np, Build build, 
 // points, children and last-face fractions are clip_bary_serial's; a lane's
 // piece stays in registers (the vertex permutation and the child patterns
 // are selects, not indexed loads).
-constexpr int kBaryPool = 64;  // pieces per warp pool
+constexpr int kBaryPool = 128;  // pieces per warp pool
 constexpr int kBaryList = 64;  // partial cells per warp list
 
 struct BaryPool {
