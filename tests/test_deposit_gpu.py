@@ -415,3 +415,35 @@ def test_particle_readers_vs_reference_fixtures(adeco, tmp_path):
         adeco.Session.from_file(str(bad), "SORTED_BY_ID")
     with pytest.raises(adeco.AdRuntimeException):
         adeco.Session.from_file(str(tmp_path / "missing.sdf"), "DARK_SKY")
+
+
+def test_clustered_zoom_requests_vs_oracle(adeco, oracle):
+    """Zoom requests over a clustered lattice (30 infall regions, many tets
+    with kappa > 32): the batch kernel's one-item CTAs and the barycentric
+    route kernel of the serving path, against the FP64 oracle per cell; a
+    request alone gives the same masses, bit for bit, as inside the batch."""
+    from adeco_gb300.synthetic import zeldovich_lattice
+    n = 40
+    pos = zeldovich_lattice(n, L=100.0, seed=6, rms_disp=3.0, infall=30)
+    flat = np.ascontiguousarray(pos.reshape(-1))
+    cd = -(-(n - 1) // 7)
+    ids = np.arange(cd ** 3, dtype=np.uint64)
+    reqs = [((50.0, 50.0, 50.0), 80.0, 32), ((30.0, 60.0, 45.0), 40.0, 24), ((65.0, 40.0, 55.0), 20.0, 40)]
+    with adeco.Session(pos) as s:
+        s.build_octree(20000, 8, leaf_dims=16)
+        _, t = s.deposit_leaves(stats=True, fetch=False)
+        assert t["routed_tets"] > 1000, t  # the lattice has ill-conditioned tets
+        b = s.submit(reqs)
+        got = [s.result(b, k, r[2]).reshape(-1) for k, r in enumerate(reqs)]
+        s.release(b)
+        b1 = s.submit([reqs[2]])
+        assert np.array_equal(s.result(b1, 0, reqs[2][2]).reshape(-1), got[2])
+        s.release(b1)
+    for k, (c, side, d) in enumerate(reqs):
+        h = np.float32(0.5) * np.float32(side)
+        box = np.array([np.float32(c[0]) - h, np.float32(c[0]) + h, np.float32(c[1]) - h, np.float32(c[1]) + h,
+                        np.float32(c[2]) - h, np.float32(c[2]) + h], np.float32)
+        ref = oracle.deposit_meta(flat, (n, n, n), ids, box, d, fp64=True)
+        bad = np.abs(got[k] - ref) > REL * np.abs(ref) + ABS
+        assert not bad.any(), (k, int(bad.sum()), float(np.abs(got[k] - ref).max()))
+        assert abs(got[k].sum() - ref.sum()) <= 1e-9 * ref.sum() + 3e-7 * np.sqrt(6 * (n - 1) ** 3) + 1e-12
