@@ -1339,42 +1339,46 @@ __device__ __forceinline__ void route_tet_warp(const float3 v[4], const int lo[3
         __syncwarp();
         if (np > kBaryList - 32) flush();
     };
-    if (ex0 < 8) {
-        const long long ncell = (long long)ex0 * ex1 * ex2;
-        for (long long c0 = 0; c0 < ncell; c0 += 32) {
+    // one loop, one offer site (so the classification and the list code are
+    // compiled once): short rows offer a cell per lane, long rows a row per
+    // lane with the cells between the row bounds (the mode is the warp's)
+    const bool by_rows = ex0 >= 8;
+    const long long ncell = (long long)ex0 * ex1 * ex2, nrows = (long long)ex1 * ex2;
+    long long c0 = 0;     // cells: first flattened cell of this round
+    long long rr = lane;  // rows: this lane's row
+    int b = 0, k = 0, a = 0, a1 = 0, a2 = 0, a3 = -1;  // the row's cells to offer: [a, a1), then [a2, a3]
+    bool active = false;
+    for (;;) {
+        bool has = false;
+        int ca = 0, cb = 0, ck = 0;
+        if (!by_rows) {
+            if (c0 >= ncell) break;
             const long long cc = c0 + lane;
-            const bool has = cc < ncell;
-            int a = 0, b = 0, k = 0;
+            c0 += 32;
+            has = cc < ncell;
             if (has) {
-                const long long rr = cc / ex0;
-                a = (int)(cc % ex0);
-                b = (int)(rr % ex1);
-                k = (int)(rr / ex1);
+                const long long q = cc / ex0;
+                ca = (int)(cc % ex0);
+                cb = (int)(q % ex1);
+                ck = (int)(q / ex1);
             }
-            offer(has, a, b, k);
-        }
-    } else {
-        const long long nrows = (long long)ex1 * ex2;
-        long long rr = lane;  // this lane's row
-        int b = 0, k = 0, a = 0, a1 = 0, a2 = 0, a3 = -1;  // cells to offer: [a, a1), then [a2, a3]
-        bool active = false;
-        for (;;) {
+        } else {
             while (!active && rr < nrows) {
                 b = (int)(rr % ex1);
                 k = (int)(rr / ex1);
                 const double ob = b * g.rcell[1], ok = k * g.rcell[2];
-                double c0 = 0.0, c1 = ex0 - 1, i0 = 0.0, i1 = ex0 - 1;
+                double lo_c = 0.0, hi_c = ex0 - 1, lo_i = 0.0, hi_i = ex0 - 1;
                 bool none = false, no_in = false;
 #pragma unroll
                 for (int f = 0; f < 4; ++f) {
                     const double nx = T.pn[f][0];
                     const double K = T.pn[f][1] * ob + T.pn[f][2] * ok - T.pd[f];
                     if (nx > 0.0) {
-                        c0 = fmax(c0, floor(-(K + T.pp[f]) * T.rnx[f]) - 1.0);
-                        i0 = fmax(i0, floor(-(K + T.pm[f]) * T.rnx[f]) + 2.0);
+                        lo_c = fmax(lo_c, floor(-(K + T.pp[f]) * T.rnx[f]) - 1.0);
+                        lo_i = fmax(lo_i, floor(-(K + T.pm[f]) * T.rnx[f]) + 2.0);
                     } else if (nx < 0.0) {
-                        c1 = fmin(c1, ceil(-(K + T.pp[f]) * T.rnx[f]) + 1.0);
-                        i1 = fmin(i1, ceil(-(K + T.pm[f]) * T.rnx[f]) - 2.0);
+                        hi_c = fmin(hi_c, ceil(-(K + T.pp[f]) * T.rnx[f]) + 1.0);
+                        hi_i = fmin(hi_i, ceil(-(K + T.pm[f]) * T.rnx[f]) - 2.0);
                     } else {
                         none = none || !(K + T.pp[f] > 0.0);
                         no_in = no_in || !(K + T.pm[f] > 0.0);
@@ -1384,8 +1388,8 @@ __device__ __forceinline__ void route_tet_warp(const float3 v[4], const int lo[3
                     rr += 32;
                     continue;
                 }
-                const int lc = (int)fmax(c0, 0.0), hc = (int)fmin(c1, (double)(ex0 - 1));
-                int li = (int)fmax(i0, (double)lc), hi_ = (int)fmin(i1, (double)hc);
+                const int lc = (int)fmax(lo_c, 0.0), hc = (int)fmin(hi_c, (double)(ex0 - 1));
+                int li = (int)fmax(lo_i, (double)lc), hi_ = (int)fmin(hi_i, (double)hc);
                 if (no_in || li > hi_) {
                     li = hc + 1;
                     hi_ = hc;
@@ -1400,18 +1404,18 @@ __device__ __forceinline__ void route_tet_warp(const float3 v[4], const int lo[3
                 if (!active) rr += 32;
             }
             if (!__any_sync(0xffffffffu, active)) break;
-            bool has = false;
-            int ca = 0;
             if (active) {
                 has = true;
                 ca = a < a1 ? a++ : a2++;
+                cb = b;
+                ck = k;
                 if (a >= a1 && a2 > a3) {
                     active = false;
                     rr += 32;
                 }
             }
-            offer(has, ca, b, k);
         }
+        offer(has, ca, cb, ck);
     }
     if (np) flush();
 }
