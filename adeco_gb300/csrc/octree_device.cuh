@@ -291,10 +291,12 @@ static int build_octree_device(const MetaGrid &mg, const float *d_mbb, const flo
     for (int a = 0; a < 3; ++a) md.cd[a] = mg.cd[a];
 
     std::vector<std::unique_ptr<DevBuf<unsigned>>> lv_ids;
-    DevBuf<unsigned long long> d_est;
-    DevBuf<TreeChunk> d_chunks;
-    DevBuf<int> d_pfc, d_cnt, d_base, d_off;
-    DevBuf<float> d_cbox;
+    // A level's small arrays share one device block and one host block, so
+    // a level costs one copy each way and the block is reallocated only when
+    // it grows (by 2x at least): est | off (brought back), chunks | pfc | cbox
+    // (sent), cnt | base (device only).
+    DevBuf<unsigned char> d_lvl;
+    std::vector<unsigned char> h_lvl;
     int rc;
 
     std::vector<BfsNode> bfs(1);
@@ -315,15 +317,16 @@ static int build_octree_device(const MetaGrid &mg, const float *d_mbb, const flo
     }
     int levels = 1;
     lv_ids.emplace_back(new DevBuf<unsigned>());
-    if ((rc = lv_ids[0]->reserve(nmc)) || (rc = d_est.reserve(1))) return rc;
-    CUDA_TRY(cudaMemsetAsync(d_est.p, 0, sizeof(unsigned long long), st));
+    if ((rc = lv_ids[0]->reserve(nmc)) || (rc = d_lvl.reserve(4096))) return rc;
     {
+        unsigned long long *d_est = reinterpret_cast<unsigned long long *>(d_lvl.p);
+        CUDA_TRY(cudaMemsetAsync(d_est, 0, sizeof(unsigned long long), st));
         TreeBox rb;
         node_box(bfs[0].n, rb.v);
         const unsigned blocks = std::min<unsigned>((nmc + 255) / 256, 4096u);
-        tree_root_kernel<<<blocks, 256, 0, st>>>(md, d_mbb, nmc, rb, lv_ids[0]->p, d_est.p);
+        tree_root_kernel<<<blocks, 256, 0, st>>>(md, d_mbb, nmc, rb, lv_ids[0]->p, d_est);
         CUDA_TRY(cudaGetLastError());
-        CUDA_TRY(cudaMemcpyAsync(&bfs[0].n.estimate, d_est.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaMemcpyAsync(&bfs[0].n.estimate, d_est, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaStreamSynchronize(st));
     }
 
@@ -331,8 +334,6 @@ static int build_octree_device(const MetaGrid &mg, const float *d_mbb, const flo
     std::vector<int> refined, pfc;
     std::vector<TreeChunk> chunks;
     std::vector<float> cbox;
-    std::vector<int> child_off;
-    std::vector<unsigned long long> child_est;
     for (int lv = 0; lv_begin < lv_end; ++lv) {
         refined.clear();
         for (size_t i = lv_begin; i < lv_end; ++i) {
@@ -391,31 +392,50 @@ static int build_octree_device(const MetaGrid &mg, const float *d_mbb, const flo
         if (cap >= (1ull << 31)) return fail(ADECO_ERR_LIMIT, "octree level lists exceed 2^31 entries");
         lv_ids.emplace_back(new DevBuf<unsigned>());
         const int nch = (int)chunks.size();
-        if ((rc = lv_ids[lv + 1]->reserve(cap)) || (rc = d_chunks.reserve(nch)) || (rc = d_pfc.reserve(pfc.size())) ||
-            (rc = d_cnt.reserve((size_t)nch * 8)) || (rc = d_base.reserve((size_t)nch * 8)) ||
-            (rc = d_off.reserve(nc + 1)) || (rc = d_est.reserve(nc)) || (rc = d_cbox.reserve(cbox.size())))
-            return rc;
-        CUDA_TRY(cudaMemcpyAsync(d_chunks.p, chunks.data(), nch * sizeof(TreeChunk), cudaMemcpyHostToDevice, st));
-        CUDA_TRY(cudaMemcpyAsync(d_pfc.p, pfc.data(), pfc.size() * sizeof(int), cudaMemcpyHostToDevice, st));
-        CUDA_TRY(cudaMemcpyAsync(d_cbox.p, cbox.data(), cbox.size() * sizeof(float), cudaMemcpyHostToDevice, st));
-        CUDA_TRY(cudaMemsetAsync(d_est.p, 0, nc * sizeof(unsigned long long), st));
-        tree_count_kernel<<<nch, kTreeThreads, 0, st>>>(d_mbb, lv_ids[lv]->p, d_chunks.p, d_cbox.p, d_cnt.p);
+        // byte offsets in the level block, each 16-byte aligned
+        const auto up = [](size_t b) { return (b + 15) & ~(size_t)15; };
+        const size_t o_est = 0, o_off = up(nc * sizeof(unsigned long long));
+        const size_t o_chunks = up(o_off + (nc + 1) * sizeof(int));
+        const size_t o_pfc = up(o_chunks + (size_t)nch * sizeof(TreeChunk));
+        const size_t o_cbox = up(o_pfc + pfc.size() * sizeof(int));
+        const size_t o_cnt = up(o_cbox + cbox.size() * sizeof(float));
+        const size_t o_base = up(o_cnt + (size_t)nch * 8 * sizeof(int));
+        const size_t bytes = up(o_base + (size_t)nch * 8 * sizeof(int));
+        if ((rc = lv_ids[lv + 1]->reserve(cap))) return rc;
+        if (bytes > d_lvl.n && (rc = d_lvl.reserve(std::max(bytes, 2 * d_lvl.n)))) return rc;
+        h_lvl.resize(std::max(h_lvl.size(), bytes));
+        std::memcpy(h_lvl.data() + o_chunks, chunks.data(), (size_t)nch * sizeof(TreeChunk));
+        std::memcpy(h_lvl.data() + o_pfc, pfc.data(), pfc.size() * sizeof(int));
+        std::memcpy(h_lvl.data() + o_cbox, cbox.data(), cbox.size() * sizeof(float));
+        unsigned char *blk = d_lvl.p;
+        unsigned long long *d_est = reinterpret_cast<unsigned long long *>(blk + o_est);
+        int *d_off = reinterpret_cast<int *>(blk + o_off);
+        const TreeChunk *d_chunks = reinterpret_cast<const TreeChunk *>(blk + o_chunks);
+        const int *d_pfc = reinterpret_cast<const int *>(blk + o_pfc);
+        const float *d_cbox = reinterpret_cast<const float *>(blk + o_cbox);
+        int *d_cnt = reinterpret_cast<int *>(blk + o_cnt);
+        int *d_base = reinterpret_cast<int *>(blk + o_base);
+        CUDA_TRY(cudaMemcpyAsync(blk + o_chunks, h_lvl.data() + o_chunks, o_cnt - o_chunks, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemsetAsync(d_est, 0, nc * sizeof(unsigned long long), st));
+        tree_count_kernel<<<nch, kTreeThreads, 0, st>>>(d_mbb, lv_ids[lv]->p, d_chunks, d_cbox, d_cnt);
         CUDA_TRY(cudaGetLastError());
-        tree_scan_kernel<<<1, 1024, 0, st>>>(d_chunks.p, nch, d_pfc.p, (int)refined.size(), d_cnt.p, d_base.p, d_off.p);
+        tree_scan_kernel<<<1, 1024, 0, st>>>(d_chunks, nch, d_pfc, (int)refined.size(), d_cnt, d_base, d_off);
         CUDA_TRY(cudaGetLastError());
-        tree_fill_kernel<<<nch, kTreeThreads, 0, st>>>(md, d_mbb, lv_ids[lv]->p, d_chunks.p, d_cbox.p, d_base.p,
-                                                        lv_ids[lv + 1]->p, d_est.p);
+        tree_fill_kernel<<<nch, kTreeThreads, 0, st>>>(md, d_mbb, lv_ids[lv]->p, d_chunks, d_cbox, d_base,
+                                                        lv_ids[lv + 1]->p, d_est);
         CUDA_TRY(cudaGetLastError());
-        child_off.resize(nc + 1);
-        child_est.resize(nc);
-        CUDA_TRY(cudaMemcpyAsync(child_off.data(), d_off.p, (nc + 1) * sizeof(int), cudaMemcpyDeviceToHost, st));
-        CUDA_TRY(cudaMemcpyAsync(child_est.data(), d_est.p, nc * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaMemcpyAsync(h_lvl.data(), blk, o_chunks, cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaStreamSynchronize(st));
         for (size_t c = 0; c < nc; ++c) {
             BfsNode &b = bfs[first_child + c];
-            b.n.estimate = child_est[c];
-            b.off = child_off[c];
-            b.len = child_off[c + 1] - child_off[c];
+            unsigned long long e;
+            int o0, o1;
+            std::memcpy(&e, h_lvl.data() + o_est + c * sizeof e, sizeof e);
+            std::memcpy(&o0, h_lvl.data() + o_off + c * sizeof(int), sizeof(int));
+            std::memcpy(&o1, h_lvl.data() + o_off + (c + 1) * sizeof(int), sizeof(int));
+            b.n.estimate = e;
+            b.off = o0;
+            b.len = o1 - o0;
         }
         lv_begin = first_child;
         lv_end = bfs.size();

@@ -842,10 +842,22 @@ extern "C" int adeco_session_create(const adeco_session_config *cfg, const float
     const long long n = (long long)nx * ny * nz;
     if ((rc = s->lattice.reserve((size_t)n))) return rc;
     {
+        // Page-locked host positions are read by the conversion kernel itself
+        // (one pass over the host link, no staging buffer); pageable ones are
+        // copied to a device staging buffer first.
+        cudaPointerAttributes at{};
+        const float *src = nullptr;
+        if (cudaPointerGetAttributes(&at, positions) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer)
+            src = static_cast<const float *>(at.devicePointer);
+        else
+            cudaGetLastError();  // clear the query's error for an unregistered pointer
         DevBuf<float> raw;
-        if ((rc = raw.reserve((size_t)n * 3))) return rc;
-        CUDA_TRY(cudaMemcpyAsync(raw.p, positions, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, s->stream));
-        xyz_to_float4_kernel<<<std::min<long long>((n + 255) / 256, 65535), 256, 0, s->stream>>>(raw.p, s->lattice.p, n);
+        if (!src) {
+            if ((rc = raw.reserve((size_t)n * 3))) return rc;
+            CUDA_TRY(cudaMemcpyAsync(raw.p, positions, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+            src = raw.p;
+        }
+        xyz_to_float4_kernel<<<std::min<long long>((n + 255) / 256, 65535), 256, 0, s->stream>>>(src, s->lattice.p, n);
         CUDA_TRY(cudaGetLastError());
         CUDA_TRY(cudaStreamSynchronize(s->stream));
     }

@@ -326,6 +326,26 @@ def test_graph_replay_matches_launch(adeco):
         assert np.array_equal(a, b)
 
 
+def test_session_from_page_locked_positions(adeco):
+    """Page-locked host positions (read by the conversion kernel directly) give
+    the same lattice and the same leaf deposits as pageable ones (copied
+    through a staging buffer)."""
+    import torch
+    g = load_golden("octree.npz")
+    n = int(g["n"])
+    pos = np.ascontiguousarray(g["positions"].reshape(n, n, n, 3), dtype=np.float32)
+    pinned = torch.empty(pos.size, dtype=torch.float32, pin_memory=True)
+    pinned.numpy()[:] = pos.reshape(-1)
+    view = pinned.numpy().reshape(n, n, n, 3)
+    out = []
+    for src in (pos, view):
+        with adeco.Session(src) as s:
+            assert np.array_equal(s.positions(), pos)
+            s.build_octree(int(g["max_tets"]), int(g["max_level"]), leaf_dims=8)
+            out.append(s.deposit_leaves()[0])
+    assert np.array_equal(out[0], out[1])
+
+
 def test_zoom_batch_same_alone_and_in_mix(adeco):
     from adeco_gb300.synthetic import zeldovich_lattice
     pos = zeldovich_lattice(24, L=40.0, seed=7, rms_disp=2.0)
