@@ -677,9 +677,9 @@ extern "C" int adeco_session_submit(adeco_session *s, const adeco_request *reqs,
         off += (long long)d * d * d;
     }
     j.cells = (size_t)off;
-    // priority class from the expected pairs (128^3 requests: side below ~4
-    // lattice spacings' worth of units take ~1-5 ms alone, up to ~15 units
-    // ~13 ms, larger ~24 ms on a GB300)
+    // priority class from the expected pairs (128^3 requests over a 256^3
+    // lattice in a box of 100 units: sides of 2 / 10 / 20 / 50 units take
+    // about 1 / 4 / 8 / 15 ms alone on a GB300)
     j.level = j.est_pairs < kClassPairs[0] ? 0 : (j.est_pairs < kClassPairs[1] ? 1 : 2);
     // layout of the job's block
     // route list: the allocating paths' rule (an eighth of a whole meta-cell's
