@@ -50,7 +50,18 @@ struct MetaGrid {
     void range(uint64_t id, int org[3], int nv[3]) const
     {
         const uint64_t nb = (uint64_t)cd[0], nb2 = nb * (uint64_t)cd[1];
-        const int c[3] = {(int)(id % nb), (int)((id % nb2) / nb), (int)(id / nb2)};
+        int c[3];
+        if (id < (1ull << 32) && nb2 < (1ull << 32)) {  // every lattice that fits a GPU: 32-bit divisions
+            const uint32_t i = (uint32_t)id, b = (uint32_t)nb, b2 = (uint32_t)nb2;
+            const uint32_t z = i / b2, r = i - z * b2, y = r / b;
+            c[0] = (int)(r - y * b);
+            c[1] = (int)y;
+            c[2] = (int)z;
+        } else {
+            c[0] = (int)(id % nb);
+            c[1] = (int)((id % nb2) / nb);
+            c[2] = (int)(id / nb2);
+        }
         const int n[3] = {nx, ny, nz};
         for (int a = 0; a < 3; ++a) {
             org[a] = c[a] * kMetaCubes;

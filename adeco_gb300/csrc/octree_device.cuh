@@ -488,6 +488,9 @@ static int build_octree_device(const MetaGrid &mg, const float *d_mbb, const flo
     }
     CUDA_TRY(cudaStreamSynchronize(st));
     tree.leaf_meta_off.reserve(tree.leaves.size() + 1);
+    size_t total = 0;
+    for (int32_t l : tree.leaves) total += (size_t)bfs[bfs_of[l]].len;
+    tree.leaf_meta_ids.reserve(total);
     int64_t off = 0;
     for (int32_t l : tree.leaves) {
         const BfsNode &b = bfs[bfs_of[l]];

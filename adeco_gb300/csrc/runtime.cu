@@ -918,8 +918,9 @@ extern "C" int adeco_session_build_octree(adeco_session *s, const float *box6, c
     const size_t nl = s->tree.leaves.size();
     const long long cells = (long long)leaf_dims * leaf_dims * leaf_dims;
     s->leaf_grids.resize(nl);
-    s->leaf_items.clear();
-    s->cube_off.clear();
+    const size_t n_items = (size_t)s->tree.leaf_meta_off[nl];
+    s->leaf_items.resize(n_items);
+    s->cube_off.resize(n_items + 1);
     long long cubes = 0;
     for (size_t q = 0; q < nl; ++q) {
         const OctNode &nd = s->tree.nodes[s->tree.leaves[q]];
@@ -930,16 +931,15 @@ extern "C" int adeco_session_build_octree(adeco_session *s, const float *box6, c
         for (int64_t k = m0; k < m1; ++k) {
             int org[3], nv[3];
             s->meta.range(s->tree.leaf_meta_ids[k], org, nv);
-            Item it;
+            Item &it = s->leaf_items[k];
             it.base = org[0] + (long long)s->nx * (org[1] + (long long)s->ny * org[2]);
             it.grid = (int)q;
             it.nv = nv[0] | (nv[1] << 8) | (nv[2] << 16);
-            s->leaf_items.push_back(it);
-            s->cube_off.push_back(cubes);
+            s->cube_off[k] = cubes;
             cubes += (long long)(nv[0] - 1) * (nv[1] - 1) * (nv[2] - 1);
         }
     }
-    s->cube_off.push_back(cubes);
+    s->cube_off[n_items] = cubes;
     int rc;
     s->out_values = nl * (size_t)cells;
     s->route_cap = route_capacity((long long)s->leaf_items.size());
