@@ -1530,6 +1530,58 @@ __global__ void fixed_to_f64_kernel(const unsigned long long *in, double *out, l
         out[i] = (double)in[i] * scale;
 }
 
+// Bounding box of the vertices of a patch slice (3 floats each), padding
+// vertices (all three coordinates 666) left out: per block min xyz, max xyz
+// and a NaN flag (7 floats) into part[blockIdx.x * 7 ...].  A cell a tet
+// deposits into lies in the tet's candidate range, inside the box of its
+// vertices, so the cells outside this box's range receive nothing.
+constexpr int kBoxThreads = 256;
+__global__ void __launch_bounds__(kBoxThreads) patch_bbox_kernel(const float *pos, long long nvert, float *part)
+{
+    float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    float nan = 0.f;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nvert; i += (long long)gridDim.x * blockDim.x) {
+        const float x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+        if (x == 666.f && y == 666.f && z == 666.f) continue;
+        if (x != x || y != y || z != z) nan = 1.f;
+        mn[0] = fminf(mn[0], x); mn[1] = fminf(mn[1], y); mn[2] = fminf(mn[2], z);
+        mx[0] = fmaxf(mx[0], x); mx[1] = fmaxf(mx[1], y); mx[2] = fmaxf(mx[2], z);
+    }
+    __shared__ float red[kBoxThreads / 32][7];
+    float v[7] = {mn[0], mn[1], mn[2], mx[0], mx[1], mx[2], nan};
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int q = 0; q < 7; ++q) {
+            const float w = __shfl_down_sync(0xffffffffu, v[q], o);
+            v[q] = (q < 3) ? fminf(v[q], w) : fmaxf(v[q], w);
+        }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0)
+        for (int q = 0; q < 7; ++q) red[warp][q] = v[q];
+    __syncthreads();
+    if (threadIdx.x < 7) {
+        const int q = threadIdx.x;
+        float r = red[0][q];
+        for (int w = 1; w < kBoxThreads / 32; ++w) r = (q < 3) ? fminf(r, red[w][q]) : fmaxf(r, red[w][q]);
+        part[blockIdx.x * 7 + q] = r;
+    }
+}
+
+// Cells [lo, lo + ext) of a dims^3 grid, packed x fastest: from the fixed
+// point grid (times scale) when `fixed` is set, else copied from `f64`.
+__global__ void grid_box_kernel(const unsigned long long *fixed, const double *f64, double *out, int dims, int lo0,
+                                int lo1, int lo2, int e0, int e1, int e2, double scale)
+{
+    const long long n = (long long)e0 * e1 * e2;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const long long r = i / e0;
+        const int x = (int)(i - r * e0), y = (int)(r % e1), z = (int)(r / e1);
+        const long long c = (lo0 + x) + (long long)dims * ((lo1 + y) + (long long)dims * (lo2 + z));
+        out[i] = fixed ? (double)fixed[c] * scale : f64[c];
+    }
+}
+
 __global__ void fixed_accumulate_f64_kernel(const unsigned long long *in, double *out, long long n, double scale)
 {
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)

@@ -337,18 +337,21 @@ struct BoundaryWork {
     DevBuf<int> counter;
     DevBuf<long long> cube_off;
     DevBuf<unsigned long long> route, fixed;
-    DevBuf<double> f64;
-    DevBuf<float> pos;
+    DevBuf<double> f64, packed;
+    DevBuf<float> pos, part;
     double *pinned = nullptr;  // D2H staging of the grid
     size_t pinned_n = 0;
+    float *pin_part = nullptr;  // D2H staging of the vertex-box partials
     ~BoundaryWork() { drop(); }
     void drop()
     {
         items.release(); grid.release(); counter.release(); cube_off.release();
-        route.release(); fixed.release(); f64.release(); pos.release();
+        route.release(); fixed.release(); f64.release(); packed.release(); pos.release(); part.release();
         if (pinned) cudaFreeHost(pinned);
         pinned = nullptr;
         pinned_n = 0;
+        if (pin_part) cudaFreeHost(pin_part);
+        pin_part = nullptr;
         if (stream) cudaStreamDestroy(stream);
         stream = nullptr;
     }
@@ -361,6 +364,14 @@ struct BoundaryWork {
         CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
         return ADECO_OK;
     }
+    int box_staging()
+    {
+        if (pin_part) return ADECO_OK;
+        if (int rc = part.reserve(kBoxBlocks * 7)) return rc;
+        CUDA_TRY(cudaHostAlloc((void **)&pin_part, kBoxBlocks * 7 * sizeof(float), cudaHostAllocDefault));
+        return ADECO_OK;
+    }
+    static constexpr int kBoxBlocks = 256;
     int staging(size_t n)
     {
         if (n <= pinned_n) return ADECO_OK;
@@ -476,6 +487,13 @@ extern "C" int adeco_deposit_tets_ex(const adeco_deposit_args *a)
     }
     // the fixed-point scale is fixed for the whole call
     const int call_shift = choose_shift(6.0 * (double)a->num_patches * (double)m * m * m, a->tet_mass);
+    // the box of the deposited vertices (padding left out), over all passes:
+    // only the grid cells in its range can receive mass, so only those are
+    // brought back and added (an image box of a periodic volume touches a
+    // thin slab of the grid)
+    float vmin[3] = {INFINITY, INFINITY, INFINITY}, vmax[3] = {-INFINITY, -INFINITY, -INFINITY};
+    bool vnan = false;
+    if (!rc) rc = t_work.box_staging();
     for (size_t done = 0; !rc && done < a->num_patches; done += per_pass) {
         const size_t np = std::min(per_pass, a->num_patches - done);
         const float *src = a->positions + (a->patch_offset + done) * fpp;
@@ -483,33 +501,89 @@ extern "C" int adeco_deposit_tets_ex(const adeco_deposit_args *a)
             rc = fail(ADECO_ERR_CUDA, "H2D positions");
             break;
         }
+        const long long nvert = (long long)(np * fpp / 3);
+        const int bb_blocks = (int)std::min<long long>(BoundaryWork::kBoxBlocks, (nvert + kBoxThreads - 1) / kBoxThreads);
+        patch_bbox_kernel<<<bb_blocks, kBoxThreads, 0, st>>>(d_pos.p, nvert, t_work.part.p);
+        if (cudaGetLastError() != cudaSuccess ||
+            cudaMemcpyAsync(t_work.pin_part, t_work.part.p, (size_t)bb_blocks * 7 * sizeof(float), cudaMemcpyDeviceToHost,
+                            st) != cudaSuccess) {
+            rc = fail(ADECO_ERR_CUDA, "vertex box");
+            break;
+        }
         // every pass uses the call's shift: deposit patches [0, np) of the slice
         rc = deposit_device_core(dev, d_pos.p, 0, np, m, a->bbox, a->dims, a->precision, a->tet_order, a->tet_mass,
                                  d_fixed.p, d_f64.p, call_shift, st);
-    }
-    // convert and add into the caller's grid on the device
-    if (!rc) {
-        const int blocks = 1024;
-        if (a->precision == ADECO_PREC_FP64) {
-            // FP64 plain path accumulated directly in FP64
-        } else {
-            if ((rc = d_f64.reserve(ncell)) == ADECO_OK)
-                fixed_to_f64_kernel<<<blocks, 256, 0, st>>>(d_fixed.p, d_f64.p, (long long)ncell,
-                                                            std::ldexp(1.0, -call_shift));
+        if (rc) break;  // deposit_device_core synchronised the stream: the partials are in
+        for (int b = 0; b < bb_blocks; ++b) {
+            const float *q = t_work.pin_part + 7 * b;
+            for (int x = 0; x < 3; ++x) {
+                vmin[x] = std::fmin(vmin[x], q[x]);
+                vmax[x] = std::fmax(vmax[x], q[3 + x]);
+            }
+            vnan = vnan || q[6] != 0.f;
         }
-        if (!rc) rc = t_work.staging(ncell);
+    }
+    // the cell range of the vertex box (one cell of margin against the
+    // rounding of the kernels' FP32 range arithmetic); a NaN coordinate
+    // falls back to the whole grid
+    int lo[3] = {0, 0, 0}, ext[3] = {a->dims, a->dims, a->dims};
+    bool empty = false;
+    if (!rc && !vnan) {
+        for (int x = 0; x < 3; ++x) {
+            const double gmin = a->bbox[2 * x], gmax = a->bbox[2 * x + 1];
+            const double delta = (double)((a->bbox[2 * x + 1] - a->bbox[2 * x]) / (float)a->dims);
+            if (!(vmin[x] <= vmax[x]) || (double)vmax[x] < gmin || (double)vmin[x] > gmax || !(delta > 0.0)) {
+                empty = true;
+                break;
+            }
+            const double flo = std::floor((std::fmax((double)vmin[x], gmin) - gmin) / delta) - 1.0;
+            const double fhi = std::ceil((std::fmin((double)vmax[x], gmax) - gmin) / delta) + 1.0;
+            const int l = (int)std::fmin(std::fmax(flo, 0.0), (double)(a->dims - 1));
+            const int h = (int)std::fmin(std::fmax(fhi, 0.0), (double)(a->dims - 1));
+            lo[x] = l;
+            ext[x] = h - l + 1;
+        }
+    }
+    // convert the box's cells to FP64 packed, bring them back, add them into
+    // the caller's grid
+    if (!rc && !empty) {
+        const size_t nbox = (size_t)ext[0] * ext[1] * ext[2];
+        const bool whole = nbox == ncell;
+        const double *dsrc = nullptr;  // device FP64 of the box, packed
+        if (a->precision == ADECO_PREC_FP64 && whole) {
+            dsrc = d_f64.p;  // the plain FP64 path accumulates in FP64: the grid itself
+        } else {
+            DevBuf<double> &dst = (a->precision == ADECO_PREC_FP64) ? t_work.packed : d_f64;
+            if ((rc = dst.reserve(nbox)) == ADECO_OK) {
+                const unsigned blocks = (unsigned)std::min<size_t>(1024, (nbox + 255) / 256);
+                grid_box_kernel<<<blocks, 256, 0, st>>>(a->precision == ADECO_PREC_FP64 ? nullptr : d_fixed.p, d_f64.p,
+                                                        dst.p, a->dims, lo[0], lo[1], lo[2], ext[0], ext[1], ext[2],
+                                                        std::ldexp(1.0, -call_shift));
+                dsrc = dst.p;
+            }
+        }
+        if (!rc) rc = t_work.staging(nbox);
         if (!rc) {
             const double *host = t_work.pinned;
-            if (cudaMemcpyAsync(t_work.pinned, d_f64.p, ncell * sizeof(double), cudaMemcpyDeviceToHost, st) !=
+            if (cudaGetLastError() != cudaSuccess ||
+                cudaMemcpyAsync(t_work.pinned, dsrc, nbox * sizeof(double), cudaMemcpyDeviceToHost, st) !=
                     cudaSuccess ||
                 cudaStreamSynchronize(st) != cudaSuccess) {
                 rc = fail(ADECO_ERR_CUDA, "D2H grid: %s", cudaGetErrorString(cudaGetLastError()));
-            } else if (a->out_type == ADECO_OUT_F64) {
-                double *out = (double *)a->data;
-                for (size_t c = 0; c < ncell; ++c) out[c] += host[c];
             } else {
-                float *out = (float *)a->data;
-                for (size_t c = 0; c < ncell; ++c) out[c] += (float)host[c];
+                const size_t d = (size_t)a->dims;
+                for (int z = 0; z < ext[2]; ++z)
+                    for (int y = 0; y < ext[1]; ++y) {
+                        const double *row = host + (size_t)ext[0] * (y + (size_t)ext[1] * z);
+                        const size_t c0 = (size_t)lo[0] + d * ((size_t)(lo[1] + y) + d * (size_t)(lo[2] + z));
+                        if (a->out_type == ADECO_OUT_F64) {
+                            double *out = (double *)a->data + c0;
+                            for (int x = 0; x < ext[0]; ++x) out[x] += row[x];
+                        } else {
+                            float *out = (float *)a->data + c0;
+                            for (int x = 0; x < ext[0]; ++x) out[x] += (float)row[x];
+                        }
+                    }
             }
         }
     }

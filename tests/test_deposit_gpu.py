@@ -94,6 +94,43 @@ def test_reference_boundary_accumulates_float(adeco):
     assert np.abs(first - g["grid_f64"]).max() <= err_ref + 1e-6
 
 
+@pytest.mark.parametrize("precision", [0, 1], ids=["mixed", "plain_fp64"])
+@pytest.mark.parametrize("out_dtype", [np.float64, np.float32], ids=["f64", "f32"])
+def test_boundary_adds_only_the_vertex_box(adeco, oracle, precision, out_dtype):
+    """A cubic grid larger than the lattice (the vertices fill part of it
+    along each axis): the call brings back and adds only the cells of the
+    vertices' box, so a pre-filled grid gains the fresh deposit there and
+    keeps every other cell; the fresh deposit matches the FP64 oracle.  (The
+    plain FP64 path sums with FP64 atomics, so two calls agree to rounding,
+    not bit for bit.)"""
+    g = load_golden("lattice_lat12_d3.npz")
+    m = int(g["m"])
+    bb = g["bbox"].astype(np.float64)
+    ext = bb[1::2] - bb[0::2]
+    below = np.array([1.5, 0.0, 0.7]) * ext  # the lattice in the upper part along x, the lower along y
+    grid = np.empty(6, np.float32)
+    grid[0::2] = bb[0::2] - below
+    grid[1::2] = bb[0::2] - below + 2.5 * ext  # cubic cells: the same extent along every axis
+    dims = 40
+    fresh = adeco.deposit_tets_ex(g["positions"], m, grid, dims, precision=precision,
+                                  data=np.zeros(dims ** 3, out_dtype))
+    ref = oracle.deposit_patches(g["positions"], m, grid, dims, fp64=True)
+    tol = dict(rel=REL, abs_=ABS) if precision == 0 else dict(rel=1e-10, abs_=1e-12)
+    if out_dtype == np.float32:
+        tol = dict(rel=1e-6 + REL, abs_=1e-6)
+    nt = 6 * m ** 3 if (precision == 0 or out_dtype == np.float32) else 0
+    check_cells(fresh.astype(np.float64), ref, n_tets=nt, **tol)
+    assert np.count_nonzero(fresh) < dims ** 3 // 4
+    pre = np.random.default_rng(3).uniform(0.5, 2.0, dims ** 3).astype(out_dtype)
+    got = adeco.deposit_tets_ex(g["positions"], m, grid, dims, precision=precision, data=pre.copy())
+    outside = fresh == 0
+    assert np.array_equal(got[outside], pre[outside])
+    if precision == 0:
+        assert np.array_equal(got, pre + fresh)
+    else:
+        assert np.allclose(got, pre + fresh, rtol=1e-12 if out_dtype == np.float64 else 1e-6, atol=0)
+
+
 def test_padded_patch_sequence(adeco, oracle):
     g = load_golden("patches_padded.npz")
     m, dims = int(g["m"]), int(g["dims"])
