@@ -557,7 +557,7 @@ constexpr int kPool = 56;    // pieces per warp pool (2 CTAs of 8 warps fit in a
 constexpr int kPairs = 128;  // partial pairs per warp list
 
 struct WarpPool {
-    float v[12][kPool];
+    float4 v[kPool][3];       // a piece's 12 coordinates per slot: 48 bytes, moved as three 16-byte words
     uint32_t meta[kPool];     // owner | faces done << 8
     long long vacc[kPairs];   // 6x volume of each listed pair, fixed point 2^kVolShift
 };
@@ -587,7 +587,13 @@ __device__ __forceinline__ void clip_pairs(WarpPool &pool, int np, Build build, 
             if (rank < top) {
                 const int idx = top - 1 - rank;
 #pragma unroll
-                for (int x = 0; x < 12; ++x) p[x] = pool.v[x][idx];
+                for (int w = 0; w < 3; ++w) {
+                    const float4 q = pool.v[idx][w];
+                    p[4 * w] = q.x;
+                    p[4 * w + 1] = q.y;
+                    p[4 * w + 2] = q.z;
+                    p[4 * w + 3] = q.w;
+                }
                 const uint32_t m = pool.meta[idx];
                 owner = (int)(m & 0xff);
                 done = (int)(m >> 8);
@@ -641,15 +647,19 @@ __device__ __forceinline__ void clip_pairs(WarpPool &pool, int np, Build build, 
                 for (int x = 0; x < 12; ++x) p[x] = c0[x];
                 done |= 1 << f;
                 if (push) {
-                    const int base = top + 2 * prank;
+                    // second children in one block, third children in the
+                    // next: consecutive pushing lanes write slots 48 bytes
+                    // apart, which spreads a quarter-warp's 16-byte words
+                    // over all banks
+                    const int s1 = top + prank, s2 = top + nfit + prank;
                     const uint32_t m = (uint32_t)owner | ((uint32_t)done << 8);
 #pragma unroll
-                    for (int x = 0; x < 12; ++x) {
-                        pool.v[x][base] = c1[x];
-                        pool.v[x][base + 1] = c2[x];
+                    for (int w = 0; w < 3; ++w) {
+                        pool.v[s1][w] = make_float4(c1[4 * w], c1[4 * w + 1], c1[4 * w + 2], c1[4 * w + 3]);
+                        pool.v[s2][w] = make_float4(c2[4 * w], c2[4 * w + 1], c2[4 * w + 2], c2[4 * w + 3]);
                     }
-                    pool.meta[base] = m;
-                    pool.meta[base + 1] = m;
+                    pool.meta[s1] = m;
+                    pool.meta[s2] = m;
                 }
             } else {
                 // finished, or at its last crossed face: the inside part
