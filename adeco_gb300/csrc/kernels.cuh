@@ -1523,13 +1523,6 @@ __global__ void tet_records_kernel(const float *patches, int m, long long cube_b
     }
 }
 
-// fixed point -> FP64 mass (and optionally += into an FP32 grid)
-__global__ void fixed_to_f64_kernel(const unsigned long long *in, double *out, long long n, double scale)
-{
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        out[i] = (double)in[i] * scale;
-}
-
 // Bounding box of the vertices of a patch slice (3 floats each), padding
 // vertices (all three coordinates 666) left out: per block min xyz, max xyz
 // and a NaN flag (7 floats) into part[blockIdx.x * 7 ...].  A cell a tet
@@ -1582,16 +1575,11 @@ __global__ void grid_box_kernel(const unsigned long long *fixed, const double *f
     }
 }
 
+// fixed-point sums -> FP64 masses, added into an FP64 grid
 __global__ void fixed_accumulate_f64_kernel(const unsigned long long *in, double *out, long long n, double scale)
 {
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
         out[i] += (double)in[i] * scale;
-}
-
-__global__ void fixed_accumulate_f32_kernel(const unsigned long long *in, float *out, long long n, double scale)
-{
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        out[i] = __fadd_rn(out[i], (float)((double)in[i] * scale));
 }
 
 // per-leaf fixed-point grids -> FP64 with each grid's own scale
