@@ -5,6 +5,7 @@ import ctypes
 import os
 import subprocess
 
+import numpy as np
 import pytest
 
 from adeco_gb300 import _lib as L
@@ -41,6 +42,40 @@ def test_abi_version(lib):
 
 def test_last_error_is_empty_string_initially(lib):
     assert isinstance(lib.adeco_last_error(), bytes)
+
+
+def test_boundary_argument_errors_on_the_host(lib):
+    """The reference's AdRuntimeException cases (AdDeposit2Grid.cu:260-268,
+    338-346; AdDeposit2Grid.cpp:95-98) and its silent return on empty input
+    (AdDeposit2Grid.cpp:86-87) are decided on the host before any device call:
+    the same status codes with or without a GPU, and the caller's grid is
+    left untouched."""
+    from adeco_gb300 import deposit as D
+    from conftest import load_golden
+    g = load_golden("lattice_lat9_d0.5.npz")
+    m, dims = int(g["m"]), int(g["dims"])
+    pos = np.ascontiguousarray(g["positions"], np.float32).reshape(-1)
+    bbox = g["bbox"]
+    data = np.full(dims ** 3, 7.0, np.float32)
+    cases = [
+        (dict(patch_offset=1, num_patches=1), 6),                                     # inconsistent offset
+        (dict(patch_offset=0, num_patches=1, positions_size=pos.size - 3), 1),        # not a whole number of patches
+        (dict(patch_offset=0, num_patches=1 << 26), 2),                               # int overflow of the cube counter
+    ]
+    for kw, code in cases:
+        with pytest.raises(D.AdRuntimeException) as e:
+            D.DepositWrapper.deposit_tets(False, 0, kw["patch_offset"], kw["num_patches"], pos,
+                                          kw.get("positions_size", pos.size), m, bbox, dims, data)
+        assert e.value.code == code, (kw, e.value)
+    with pytest.raises(D.AdRuntimeException) as e:  # an empty bbox axis
+        D.DepositWrapper.deposit_tets(False, 0, 0, 1, pos, pos.size, m, np.zeros(6, np.float32), dims, data)
+    assert e.value.code == 1
+    with pytest.raises(D.AdRuntimeException) as e:  # an unknown precision
+        D.deposit_tets_ex(pos, m, bbox, dims, data=np.zeros(dims ** 3), precision=7)
+    assert e.value.code == 1
+    D.DepositWrapper.deposit_tets(False, 0, 0, 0, pos, pos.size, m, bbox, dims, data)  # empty: a no-op
+    D.DepositWrapper.deposit_tets(False, 0, 0, 1, pos, 0, m, bbox, dims, data)
+    assert np.all(data == 7.0)
 
 
 def test_cpp_wrapper_header_compiles(tmp_path):
